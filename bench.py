@@ -1,0 +1,339 @@
+"""Benchmark: cell-updates/s of the force-free SSP-RK3 step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--size S] [--precision fp32|fp32c|fp64] [--no-cpu-baseline]
+
+Workload (the single-grid benchmark configuration): a periodic S^3 grid
+(S = 512), Bz = 1 plus 32 seeded Alfven and fast modes with integer
+wavevectors |k| <= 8 and amplitudes U[0, 0.02], c = 0.45, FP32 fields.
+A step is one full main-loop body: three SSP-RK3 stages, each with its E
+cleaning and ghost fills.  One cell-update = one interior cell advanced one
+step.  Inputs are 3.3 GB per field set, far larger than the 129 MB L2, so no
+flush is needed between steps.
+
+Reported numbers:
+  value   : cell-updates/s with the fields resident in HBM (CUDA events on the
+            library's stream around K steps; max over ranks).
+  e2e     : the same metric through the C ABI from pinned host buffers:
+            upload of E,B, K steps, download of E,B, all inside the timed region.
+  roofline: the fused stage kernel (3 launches per step, the whole step):
+            algorithmic bytes = 48 words per cell-update (stage 1 reads E,B and
+            writes E,B; stages 2-3 also read the step-start E,B) / step time,
+            against the measured HBM copy bandwidth.
+  cpu_baseline: the CPU restatement (oracle/, OpenMP, all host cores) on a
+            bounded sample of the same workload.
+Multi-GPU: replicas only (one independent grid per rank, no collective in the
+data path); value sums all ranks' cell-updates over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tristan-ff_gb300"))
+
+WORDS_PER_CELL_STEP = 48      # fused path: 12 + 18 + 18 words per cell per step
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", HBM_FALLBACK_GBS)), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def traffic_from_profile(precision, size):
+    """DRAM bytes per fused-stage launch from the committed ncu summary, scaled to `size`."""
+    p = os.path.join(ROOT, "profiles", "fused_stage_traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        e = d.get(precision)
+        if not e:
+            return None
+        return e["bytes_per_cell_per_launch"] * size ** 3
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index) if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/ffe_clocks_%d.csv" % os.getpid()
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+            rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+            sm = [float(r[1]) for r in rows]
+            mx = max(float(r[2]) for r in rows)
+            reasons = set()
+            names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+            for r in rows:
+                for n, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                    "samples": len(rows)}
+        except Exception as e:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)[:80]}
+
+
+def workload(size):
+    from ffe.workloads import random_modes
+    bg, modes, meta = random_modes((size, size, size), seed=1, n=32, kmax=8, amax=0.02)
+    return bg, modes
+
+
+def cpu_baseline(args, edge=None, steps=None, threads=None):
+    """Time the oracle (CPU restatement) on an edge^3 grid of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import ffe
+    import oracle as O
+    from ffe.workloads import random_modes, host_waves
+    O.build()
+    threads = threads or os.cpu_count() or 1
+    edge = edge or args.cpu_sample or 128
+    steps = steps or 2
+    size = (edge, edge, edge)
+    bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
+    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
+    o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
+    o.mainloop_prologue()
+    o.mainloop(1, 0)  # warm caches and pages
+    t0 = time.perf_counter()
+    o.mainloop(steps, 1)
+    dt = time.perf_counter() - t0
+    return {"value": edge ** 3 * steps / dt, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d^3 grid of the same random-mode workload, %d steps, %s, x-innermost loops, "
+                      "OpenMP %d threads, %.1f s" % (edge, steps, args.precision, threads, dt)}
+
+
+def run_reference(args):
+    """The reference's CPU path: its Fortran build is unavailable here, so the
+    CPU restatement of the same procedures (oracle/) runs on all host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    edge = args.cpu_sample or 128
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ffe
+    import oracle as O
+    from ffe.workloads import random_modes, host_waves
+    O.build()
+    threads = os.cpu_count() or 1
+    size = (edge, edge, edge)
+    bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
+    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
+    o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
+    o.mainloop_prologue()
+    o.mainloop(args.warmup, 0)
+    t0 = time.perf_counter()
+    o.mainloop(args.steps, args.warmup)
+    dt = time.perf_counter() - t0
+    v = edge ** 3 * args.steps / dt
+    cfg = {"workload": "random Alfven+fast modes, periodic %d^3 (CPU sample %d^3)" % (args.size, edge),
+           "grid": [args.size] * 3, "modes": 32, "kmax": 8, "amax": 0.02, "cc": 0.45,
+           "boundary": "periodic", "parallelism": "replicas" if world > 1 else "single grid"}
+    line = {"metric": "cell-updates/s per RK3 step", "value": v, "unit": "cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": "%d^3 grid, %d steps after %d warm-up; the reference's Fortran build "
+                                       "is unavailable (no Fortran compiler, MPI, HDF5), so its CPU "
+                                       "restatement runs" % (edge, args.steps, args.warmup)},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+    import ffe
+    import build as ffe_build
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if rank == 0:
+        ffe_build.build()
+    if world > 1:
+        dist.barrier()
+
+    S = args.size
+    size = (S, S, S)
+    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    stream = torch.cuda.Stream()
+    desc = ffe.make_desc(size, precision=prec, stream=stream.cuda_stream)
+    g = ffe.Solver(desc)
+    bg, modes = workload(S)
+    g.init_waves(bg, modes)
+    g.mainloop_prologue()
+    g.synchronize()
+    launches_per_step = g.step_launches()
+
+    # ---- device-resident timing -------------------------------------------
+    step = 0
+    g.mainloop(args.warmup, step)
+    step += args.warmup
+    g.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        g.mainloop(args.steps, step)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    step += args.steps
+    t_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    ok = g.check_finite()
+    cells = S ** 3
+    ms_per_step = t_ms / args.steps
+    value = cells * args.steps * world / (t_ms / 1e3)
+
+    # ---- end to end through the C ABI from pinned host buffers ------------
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+    dt = np.float64 if prec == ffe.FP64 else np.float32
+    host = {}
+    for n in names:
+        t = torch.empty(g.shape, dtype=torch.float64 if dt == np.float64 else torch.float32, pin_memory=True)
+        a = t.numpy()
+        host[n] = (t, a)
+    g2 = ffe.Solver(ffe.make_desc(size, precision=prec, stream=stream.cuda_stream))
+    g2.init_waves(bg, modes)
+    for n in names:
+        host[n][1][...] = g2.download(n)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for n in names:
+        g2.upload(n, host[n][1])
+    g2.mainloop_prologue()
+    g2.mainloop(args.steps, 0)
+    for n in names:
+        g2._ck(g2.lib.ffe_download(g2.h, ffe.FIELD_ID[n], host[n][1].ctypes.data, host[n][1].size), "download")
+    g2.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    arr_bytes = host["ex"][1].nbytes
+    e2e = {"value": cells * args.steps * world / e2e_s, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": 6 * arr_bytes / args.steps, "d2h_bytes_per_step": 6 * arr_bytes / args.steps,
+           "note": "upload E,B + %d steps + download E,B per run, from pinned host memory" % args.steps}
+    g2.close()
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+        return
+    peak, peak_kind = peaks()
+    es = 8 if prec == ffe.FP64 else 4
+    alg_bytes_step = cells * WORDS_PER_CELL_STEP * es
+    achieved = alg_bytes_step / (ms_per_step / 1e3) / 1e9
+    traffic = traffic_from_profile(args.precision, S)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "k_fused (fused stage, %d launches/step = whole step)" % launches_per_step,
+            "alg_bytes_per_launch": alg_bytes_step / 3, "peak_source": peak_kind + " copy bandwidth"}
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            cpu = cpu_baseline(args)
+        except Exception as e:
+            cpu = {"value": None, "error": str(e)[:200]}
+    clocks = clk.summary()
+    cfg = {"workload": "random Alfven+fast modes, periodic %d^3, %s" % (S, args.precision),
+           "grid": [S, S, S], "modes": 32, "kmax": 8, "amax": 0.02, "cc": 0.45, "boundary": "periodic",
+           "l2": "inputs (3.3 GB per field set) larger than L2; no flush",
+           "parallelism": "replicas x%d" % world if world > 1 else "single grid",
+           "path": "fused" if g.step_path() != ffe.PATH_STAGED else "staged"}
+    line = {"metric": "cell-updates/s per RK3 step", "value": value, "unit": "cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic", "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clocks, "gpu_launches": launches_per_step * args.steps, "finite": ok}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,199 @@
+/*
+ * ffe.h — C ABI of the GB300 force-free field solver (libffe_gb300.so).
+ *
+ * The reference (tristan-ff, Fortran 2008) exposes its field update as
+ * argument-less module procedures acting on module-global arrays.  Each entry
+ * point below replaces one of those procedures for ONE meshblock that lives
+ * on ONE GPU; the fields stay resident in device memory between calls.
+ *
+ *   reference procedure                               replaced by
+ *   -----------------------------------------------   ------------------------
+ *   m_initialize::initializeFields   (src/logistics/initialize.F90:201-229)   ffe_create
+ *   m_finalize (deallocation)        (src/logistics/finalize.F90:14-71)        ffe_destroy
+ *   m_fldsolver::initRKstep          (src/algorithms/field_solver.F90:15-33)   ffe_init_rk_step
+ *   m_fldsolver::rk3Step             (src/algorithms/field_solver.F90:35-42)   ffe_rk3_stage
+ *   m_fldsolver::computeRho          (src/algorithms/field_solver.F90:44-63)   ffe_compute_rho
+ *   m_fldsolver::rk3Push             (src/algorithms/field_solver.F90:65-166)  ffe_rk3_push
+ *   m_fldsolver::rk3Update           (src/algorithms/field_solver.F90:168-271) ffe_rk3_update
+ *   m_fldsolver::cleanEpar           (src/algorithms/field_solver.F90:273-335) ffe_clean_epar
+ *   m_exchangefields::exchangeFields (src/logistics/exchange_fields.F90:11-197) ffe_exchange_fields
+ *   m_userfile::userInitialize       (user/user_psr.F90:20-69,
+ *                                     user/user_uniform.F90:20-69,
+ *                                     user/user_loop.F90:20-93)               ffe_user_initialize
+ *   m_userfile::userFieldBoundaryConditions
+ *                                    (user/user_psr.F90:72-332,
+ *                                     user/user_uniform.F90:77-147,
+ *                                     user/user_loop.F90:101-164)             ffe_user_bc
+ *   m_mainloop::mainloop prologue    (src/tristanmainloop.F90:41-42)           ffe_mainloop_prologue
+ *   m_mainloop::mainloop step body   (src/tristanmainloop.F90:50-84)           ffe_step
+ *
+ * Array contract.  Host arrays passed to ffe_upload / ffe_download have the
+ * reference's allocation shape (src/logistics/initialize.F90:192-199):
+ * (sx+4) x (sy+4) x (sz+4) values, index range -2..s+1 per axis (NGHOST = 2,
+ * src/CMakeLists.txt:18), column-major with x fastest, element type double
+ * for FFE_FP64 and float otherwise.  A Fortran caller passes c_loc(ex).
+ *
+ * Errors.  Every function returns FFE_OK (0) or a negative ffe_status.  The
+ * message of the last failure is kept per handle (ffe_last_error) and, for
+ * failures without a handle, per host thread (ffe_last_error(NULL, ...)).
+ * The reference has no error returns: its fatal paths print and stop
+ * (src/tools/error_handling.F90:8-13).
+ *
+ * Threads and streams.  A handle is used by one host thread at a time; all
+ * of its device work is ordered on the stream given at creation (NULL = a
+ * stream the library creates).  Distinct handles may run concurrently.
+ */
+#ifndef FFE_GB300_H
+#define FFE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFE_NGHOST 2
+#define FFE_ABI_VERSION 1
+
+typedef struct ffe_solver* ffe_t;
+
+typedef enum {
+  FFE_OK = 0,
+  FFE_EINVAL = -1,      /* bad argument or descriptor                        */
+  FFE_ENOMEM = -2,      /* device or host allocation failed                  */
+  FFE_ECUDA = -3,       /* a CUDA runtime call failed                        */
+  FFE_ESTATE = -4,      /* call not valid in the handle's current state      */
+  FFE_ENONFINITE = -5,  /* ffe_check_finite found NaN/Inf                    */
+  FFE_ETIMEOUT = -6,    /* a bounded device wait gave up                     */
+  FFE_EUNSUPPORTED = -7 /* combination of options not built                  */
+} ffe_status;
+
+typedef enum {
+  FFE_FP64 = 0,  /* every real is double: what a -fdefault-real-8 build computes */
+  FFE_FP32 = 1,  /* every real is float: the arithmetic of the shipped build      */
+  FFE_FP32C = 2  /* float storage; increment-form (compensated) RK combination;
+                    B^2 denominators of the current and the cleaning in double  */
+} ffe_precision;
+
+typedef enum {
+  FFE_BOUNDARY_OPEN = 0,     /* ghosts keep their values (no neighbour)   */
+  FFE_BOUNDARY_PERIODIC = 1, /* ghosts wrap to the opposite interior      */
+  FFE_BOUNDARY_ABSORB = 2    /* spherical absorbing shell, ghosts frozen  */
+} ffe_boundary;
+
+typedef enum {
+  FFE_EX = 0, FFE_EY, FFE_EZ, FFE_BX, FFE_BY, FFE_BZ,
+  FFE_B0X, FFE_B0Y, FFE_B0Z,
+  /* the reference's work arrays, readable after the per-procedure calls
+     (src/objects/fields.F90:17-24) */
+  FFE_DEX, FFE_DEY, FFE_DEZ, FFE_DBX, FFE_DBY, FFE_DBZ,
+  FFE_ENX, FFE_ENY, FFE_ENZ, FFE_BNX, FFE_BNY, FFE_BNZ,
+  FFE_RHO,
+  FFE_NFIELDS
+} ffe_field;
+
+typedef enum {
+  FFE_SETUP_NONE = 0,    /* no user boundary condition                      */
+  FFE_SETUP_PSR = 1,     /* user/user_psr.F90: rotating conducting sphere    */
+  FFE_SETUP_UNIFORM = 2, /* user/user_uniform.F90: twisted flux tube         */
+  FFE_SETUP_LOOP = 3     /* user/user_loop.F90: magnetic loop                */
+} ffe_setup;
+
+/* Index of each setup's parameters in ffe_grid_desc.params[]:
+ *  PSR:     0 psr_radius, 1 psr_angle [deg], 2 psr_period [steps],
+ *           3 field scale (1 = the shipped |mu| = R^3, user/user_psr.F90:365-367)
+ *  UNIFORM: 0 L0, 1 r_L0, 2 t0, 3 beta_twist   (user/user_uniform.F90:29-38)
+ *  LOOP:    0 L0, 1 a_L0, 2 h_L0, 3 r_L0, 4 t0, 5 beta_twist
+ *                                              (user/user_loop.F90:29-41)   */
+#define FFE_MAX_PARAMS 8
+
+typedef enum {
+  FFE_PATH_AUTO = 0,      /* fused kernels where the setup allows, else FFE_PATH_STAGED */
+  FFE_PATH_STAGED = 1,    /* one kernel per reference procedure, reference order */
+  FFE_PATH_FUSED = 2,     /* require the fused stage+clean kernels (error if not possible) */
+  FFE_PATH_FUSED_EXACT = 3 /* the fused kernels built without multiply-add contraction:
+                              same rounding as FFE_PATH_STAGED, for verification */
+} ffe_path;
+
+typedef struct {
+  int32_t sx, sy, sz;          /* interior cells of this meshblock           */
+  int32_t x0, y0, z0;          /* meshblock corner in the global mesh        */
+  int32_t gsx, gsy, gsz;       /* global mesh size (mx0, my0, mz0)           */
+  int32_t boundary[3];         /* ffe_boundary per axis; 2 on any axis => all */
+  int32_t absorb_buff;         /* <grid> absorb_buff (default 20)            */
+  int32_t precision;           /* ffe_precision                              */
+  int32_t setup;               /* ffe_setup                                  */
+  int32_t path;                /* ffe_path                                   */
+  double cc;                   /* <algorithm> c, the Courant number          */
+  double params[FFE_MAX_PARAMS];
+  void* stream;                /* cudaStream_t to order work on, or NULL     */
+} ffe_grid_desc;
+
+/* Fill *d with the reference's defaults: periodic, c = 0.45, absorb_buff 20
+   (src/logistics/initialize.F90:139-148,185-190), the given interior size,
+   a single meshblock covering the global mesh, FFE_FP32, FFE_PATH_AUTO.    */
+int ffe_desc_default(ffe_grid_desc* d, int32_t sx, int32_t sy, int32_t sz);
+
+/* Allocate device state for one meshblock (all fields zero). */
+int ffe_create(ffe_t* out, const ffe_grid_desc* desc);
+int ffe_destroy(ffe_t h);
+
+/* Copy of the last error message; returns the status that produced it. */
+int ffe_last_error(ffe_t h, char* buf, size_t len);
+
+/* Number of elements of one ghosted host array: (sx+4)(sy+4)(sz+4). */
+int ffe_field_elems(ffe_t h, size_t* nelems);
+/* Device bytes the handle holds. */
+int ffe_device_bytes(ffe_t h, size_t* bytes);
+
+/* Host <-> device copies of one whole ghosted array (see array contract). */
+int ffe_upload(ffe_t h, int32_t field, const void* host, size_t nelems);
+int ffe_download(ffe_t h, int32_t field, void* host, size_t nelems);
+
+/* --- per-procedure operator API (reference order, one launch each) ---- */
+int ffe_init_rk_step(ffe_t h);
+int ffe_compute_rho(ffe_t h);
+int ffe_rk3_push(ffe_t h);
+int ffe_rk3_update(ffe_t h, double c1, double c2, double c3);
+int ffe_rk3_stage(ffe_t h, double c1, double c2, double c3);
+int ffe_clean_epar(ffe_t h);
+int ffe_exchange_fields(ffe_t h, int32_t exchange_b0);
+int ffe_user_initialize(ffe_t h);
+int ffe_user_bc(ffe_t h, int32_t step);
+
+/* Synthetic plane-wave workload (no counterpart among the reference's user
+   files; it builds the Alfven-packet and random-mode grids of the benchmark):
+   B = bg + sum_m dB_m, E = sum_m -n_m x dB_m, dB_m(x) = -a_m sin(K_m.x + phi_m) u_m,
+   evaluated in double at every staggered point (ghosts included), rounded once
+   to the storage precision; B0 is set to zero.  modes holds 11 doubles per mode:
+   K[3] (radians per cell), phi, a, u[3] (unit polarisation), n[3]; nmodes <= 64. */
+int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* modes);
+
+/* --- whole steps -------------------------------------------------------- */
+/* exchangeFields(exchangeB0=.true.) then userFieldBoundaryConditions(0). */
+int ffe_mainloop_prologue(ffe_t h);
+/* nsteps repetitions of the main-loop body for timesteps step0 .. step0+nsteps-1:
+   initRKstep; 3 x [rk3Step(c); user BC(timestep); exchange; cleanEpar; exchange]
+   with c = (1,0,1), (3/4,1/4,1/4), (1/3,2/3,2/3).  Asynchronous on the
+   handle's stream. */
+int ffe_step(ffe_t h, int32_t nsteps, int32_t step0);
+/* Which path ffe_step takes for this handle: FFE_PATH_STAGED or FFE_PATH_FUSED. */
+int ffe_step_path(ffe_t h, int32_t* path);
+/* Number of kernel launches one ffe_step(h, 1, .) issues. */
+int ffe_step_launches(ffe_t h, int32_t* launches);
+
+/* Sets *ok = 1 if E and B are finite over the interior, else 0 and returns
+   FFE_ENONFINITE.  Synchronises the handle's stream. */
+int ffe_check_finite(ffe_t h, int32_t* ok);
+/* Wait for the handle's stream. */
+int ffe_synchronize(ffe_t h);
+/* Wait for the handle's stream, giving up after timeout_ms (FFE_ETIMEOUT). */
+int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms);
+
+int ffe_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFE_GB300_H */

@@ -1,0 +1,61 @@
+"""CPU checks of the C-ABI library: it builds for sm_103a, loads without a GPU,
+and exports every function include/ffe.h declares (no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import ffe
+from conftest import ROOT
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "ffe.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*int\s+(ffe_\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import build as ffe_build
+    ffe_build.build()
+    return ctypes.CDLL(ffe.LIB_PATH)
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    assert "ffe_create" in names and "ffe_step" in names and len(names) >= 20
+    assert set(names) == set(ffe.ABI_SYMBOLS), set(names) ^ set(ffe.ABI_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for n in declared_functions():
+        assert hasattr(lib, n), n
+
+
+def test_abi_version_and_descriptor_defaults(lib):
+    L = ffe.load_library()
+    assert L.ffe_abi_version() == 1
+    d = ffe.GridDesc()
+    assert L.ffe_desc_default(ctypes.byref(d), 16, 8, 4) == 0
+    assert (d.sx, d.sy, d.sz, d.gsx) == (16, 8, 4, 16)
+    assert list(d.boundary) == [1, 1, 1] and d.absorb_buff == 20 and abs(d.cc - 0.45) < 1e-15
+
+
+def test_descriptor_layout_matches_header():
+    # int32 x 16, then double cc at offset 64, params, stream pointer
+    assert ffe.GridDesc.cc.offset == 64
+    assert ffe.GridDesc.params.offset == 72
+    assert ffe.GridDesc.stream.offset == 136
+    assert ctypes.sizeof(ffe.GridDesc) == 144
+
+
+def test_create_rejects_bad_descriptors_without_a_gpu(lib):
+    L = ffe.load_library()
+    h = ctypes.c_void_p()
+    d = ffe.make_desc((1, 8, 8))
+    assert L.ffe_create(ctypes.byref(h), ctypes.byref(d)) == -1
+    buf = ctypes.create_string_buffer(256)
+    assert L.ffe_last_error(None, buf, 256) == -1
+    assert b"ghost zones" in buf.value

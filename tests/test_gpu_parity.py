@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA library (through its C ABI) against the CPU oracle.
+
+Bars:
+  * staged and fused-exact paths: bit-exact with the oracle in FP64, FP32 and
+    FP32C (no multiply-add contraction on either side, IEEE division/sqrt);
+    the user boundary conditions use tanh/exp, compared with tolerances;
+  * fused fast path (contraction on): FP64 rel. L2 <= 1e-12 and FP32/FP32C
+    rel. L2 <= 1e-5 against the oracle of the same precision after 20 steps.
+"""
+import numpy as np
+import pytest
+
+import ffe
+from ffe.workloads import random_modes, alfven_packet, host_waves
+from conftest import rel_l2, rel_linf
+from test_oracle_cpu import random_fields
+
+pytestmark = pytest.mark.gpu
+
+F6 = ("ex", "ey", "ez", "bx", "by", "bz")
+PRECS = [ffe.FP64, ffe.FP32, ffe.FP32C]
+BNDS = [(1, 1, 1), (0, 0, 0), (2, 2, 2), (1, 1, 0)]
+
+
+def dtype_of(prec):
+    return np.float64 if prec == ffe.FP64 else np.float32
+
+
+def pair(oracle_mod, size, prec, bnd, path, seed=3, b0=True, **kw):
+    d = ffe.make_desc(size, precision=prec, boundary=bnd, absorb_buff=3, path=path, **kw)
+    g = ffe.Solver(d)
+    o = oracle_mod.Oracle(d)
+    f = random_fields(size, dtype_of(prec), seed=seed, e_scale=0.7, b0=b0)
+    g.set_fields(f)
+    o.set_fields(f)
+    return g, o
+
+
+def assert_same(g, o, names=F6, exact=True, tol=0.0):
+    for k in names:
+        a, b = g.download(k), o.download(k)
+        if exact:
+            bad = ~((a == b) | (np.isnan(a) & np.isnan(b)))
+            assert not bad.any(), (k, int(bad.sum()), np.argwhere(bad)[:3].tolist())
+        else:
+            assert rel_l2(a, b) <= tol, (k, rel_l2(a, b))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("bnd", BNDS)
+def test_staged_procedures_bit_exact(oracle_mod, prec, bnd):
+    """Each reference procedure alone, including the work arrays it writes."""
+    g, o = pair(oracle_mod, (13, 9, 7), prec, bnd, ffe.PATH_STAGED)
+    for s in (g, o):
+        s.exchangeFields(True)
+        s.initRKstep()
+    assert_same(g, o, F6 + ("enx", "bnz", "b0x", "b0z"))
+    for s in (g, o):
+        s.computeRho()
+    assert_same(g, o, ("rho",))
+    for s in (g, o):
+        s.rk3Push()
+    assert_same(g, o, ("dex", "dey", "dez", "dbx", "dby", "dbz"))
+    for s in (g, o):
+        s.rk3Update(0.75, 0.25, 0.25)
+    assert_same(g, o)
+    for s in (g, o):
+        s.exchangeFields()
+        s.cleanEpar()
+    assert_same(g, o, F6 + ("dex", "dey", "dez"))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("bnd", BNDS)
+@pytest.mark.parametrize("path", [ffe.PATH_STAGED, ffe.PATH_FUSED_EXACT])
+def test_steps_bit_exact(oracle_mod, prec, bnd, path):
+    g, o = pair(oracle_mod, (37, 19, 11), prec, bnd, path)
+    for s in (g, o):
+        s.mainloop_prologue()
+        s.mainloop(3, 0)
+    g.synchronize()
+    assert_same(g, o)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("bnd", [(1, 1, 1), (2, 2, 2), (0, 1, 0)])
+def test_fused_fast_matches_oracle(oracle_mod, prec, bnd):
+    size = (40, 24, 20)
+    d = ffe.make_desc(size, precision=prec, boundary=bnd, absorb_buff=4, path=ffe.PATH_FUSED)
+    g = ffe.Solver(d)
+    o = oracle_mod.Oracle(d)
+    bg, modes, _ = random_modes(size, seed=4, n=8, kmax=3, amax=0.05)
+    g.init_waves(bg, modes)
+    f = g.fields()
+    o.set_fields(f)
+    for s in (g, o):
+        s.mainloop_prologue()
+        s.mainloop(20, 0)
+    tol = 1e-12 if prec == ffe.FP64 else 1e-5
+    assert_same(g, o, exact=False, tol=tol)
+
+
+def test_fused_tiles_cover_ragged_sizes(oracle_mod):
+    """Sizes that are not multiples of the 32x8 tile or of the z chunk."""
+    for size in [(33, 9, 5), (70, 17, 13), (2, 2, 2), (5, 31, 3)]:
+        g, o = pair(oracle_mod, size, ffe.FP64, (1, 1, 1), ffe.PATH_FUSED_EXACT, b0=False)
+        for s in (g, o):
+            s.mainloop_prologue()
+            s.mainloop(2, 0)
+        assert_same(g, o)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_waves_init_matches_host(prec):
+    size = (20, 12, 10)
+    bg, modes, _ = random_modes(size, seed=9, n=5, kmax=3, amax=0.1)
+    g = ffe.Solver(ffe.make_desc(size, precision=prec))
+    g.init_waves(bg, modes)
+    ref = host_waves(size, bg, modes, np.float64)
+    tol = 1e-13 if prec == ffe.FP64 else 1e-7
+    for k in F6:
+        a = g.download(k).astype(np.float64)
+        assert np.max(np.abs(a - ref[k])) <= tol * max(1.0, np.max(np.abs(ref[k]))), k
+
+
+@pytest.mark.parametrize("setup,bnd,params", [
+    (ffe.SETUP_PSR, (0, 0, 0), (5.0, 30.0, 200.0, 1.0)),
+    (ffe.SETUP_PSR, (2, 2, 2), (5.0, 60.0, 150.0, 10.0)),
+    (ffe.SETUP_UNIFORM, (1, 1, 0), (10.0, 0.4, 5.0, 0.3)),
+    (ffe.SETUP_LOOP, (1, 1, 0), (4.0, 1.0, 1.0, 0.5, 5.0, 0.3)),
+])
+@pytest.mark.parametrize("prec", PRECS)
+def test_user_setups(oracle_mod, setup, bnd, params, prec):
+    size = (24, 24, 24)
+    d = ffe.make_desc(size, precision=prec, boundary=bnd, setup=setup, params=params, absorb_buff=4)
+    g = ffe.Solver(d)
+    o = oracle_mod.Oracle(d)
+    for s in (g, o):
+        s.userInitialize()
+    # initial fields: sqrt and division only -> bit-exact
+    assert_same(g, o, F6 + ("b0x", "b0y", "b0z"))
+    for s in (g, o):
+        s.mainloop_prologue()
+        s.mainloop(4, 0)
+    # tanh / exp of the boundary conditions round differently on the GPU
+    tol = 1e-12 if prec == ffe.FP64 else 2e-5
+    assert_same(g, o, exact=False, tol=tol)
+    assert g.check_finite()
+
+
+def test_check_finite_flags_nan():
+    size = (8, 8, 8)
+    g = ffe.Solver(ffe.make_desc(size, precision=ffe.FP32))
+    a = np.zeros(g.shape, np.float32)
+    assert g.check_finite()
+    a[5, 5, 5] = np.nan
+    g.upload("ey", a)
+    assert not g.check_finite()
+
+
+def test_errors_are_reported():
+    with pytest.raises(ffe.FFEError) as e:
+        ffe.Solver(ffe.make_desc((1, 8, 8)))
+    assert "ghost zones" in str(e.value)
+    g = ffe.Solver(ffe.make_desc((8, 8, 8), setup=ffe.SETUP_PSR, params=(2.0, 10.0, 100.0),
+                                 path=ffe.PATH_FUSED))
+    with pytest.raises(ffe.FFEError):
+        g.mainloop(1)
+    with pytest.raises(ffe.FFEError):
+        g.upload("ex", np.zeros((3, 3, 3), np.float32))
+
+
+def test_step_paths_and_launch_counts():
+    g = ffe.Solver(ffe.make_desc((16, 16, 16)))
+    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 3
+    g = ffe.Solver(ffe.make_desc((16, 16, 16), setup=ffe.SETUP_PSR, params=(3.0, 10.0, 100.0),
+                                 boundary=(0, 0, 0)))
+    assert g.step_path() == ffe.PATH_STAGED
+
+
+def test_large_grid_fp32_vs_fp64_gpu():
+    """256^3 random modes, 10 steps: FP32 and FP32C stay within 1e-5 of FP64."""
+    size = (256, 256, 256)
+    bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
+    res = {}
+    for prec in PRECS:
+        g = ffe.Solver(ffe.make_desc(size, precision=prec))
+        g.init_waves(bg, modes)
+        g.mainloop_prologue()
+        g.mainloop(10, 0)
+        res[prec] = {k: ffe.interior(g.download(k)).astype(np.float64) for k in F6}
+        g.close()
+    for prec in (ffe.FP32, ffe.FP32C):
+        eb = np.concatenate([res[prec][k].ravel() for k in F6])
+        e64 = np.concatenate([res[ffe.FP64][k].ravel() for k in F6])
+        assert rel_l2(eb, e64) < 1e-5, (prec, rel_l2(eb, e64))

@@ -1,0 +1,55 @@
+// ffe_kernels.h — host-side launchers of the device kernels (internal).
+#pragma once
+#include <algorithm>
+#include <cuda_runtime.h>
+#include "ffe_common.cuh"
+
+namespace ffe {
+
+// ---- staged kernels (ffe_staged.cu), one per reference procedure -----------
+template <typename R>
+void launch_rho(const Geom& g, const R* ex, const R* ey, const R* ez, R* rho, cudaStream_t st);
+template <typename R, bool C>
+void launch_push(const Geom& g, R cc, const CEB<R>& eb, const CEB<R>& b0, bool has_b0, const R* rho, const EB<R>& d,
+                 cudaStream_t st);
+template <typename R, bool C>
+void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2, R c3, bool incr, const EB<R>& f,
+                   const CEB<R>& fn, const CEB<R>& df, cudaStream_t st);
+template <typename R, bool C>
+void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, cudaStream_t st);
+template <typename R>
+void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st);
+template <typename R>
+void launch_psr_bc(const Geom& g, const Phys& p, const PsrBC<R>& q, const EB<R>& f, R* box, cudaStream_t st);
+template <typename R>
+void launch_uniform_bc(const Geom& g, const Phys& p, const UniformBC<R>& u, const EB<R>& f, cudaStream_t st);
+template <typename R>
+void launch_loop_bc(const Geom& g, const Phys& p, const EB<R>& f, cudaStream_t st);
+template <typename R>
+void launch_psr_init(const Geom& g, const Phys& p, const PsrBC<R>& q, const EB<R>& f, cudaStream_t st);
+template <typename R>
+void launch_uniform_init(const Geom& g, const Phys& p, const UniformBC<R>& u, R* bz, R* b0z, cudaStream_t st);
+template <typename R>
+void launch_loop_init(const Geom& g, const Phys& p, const double prm[8], const EB<R>& f, const EB<R>& f0,
+                      cudaStream_t st);
+// synthetic plane-wave workloads: 11 doubles per mode, see ffe_staged.cu
+size_t waves_param_bytes();
+template <typename R>
+int launch_waves(const Geom& g, const Phys& p, const double bg[3], int n, const double* modes, void* dparam,
+                 const EB<R>& f, cudaStream_t st);
+template <typename R>
+void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
+
+// ---- fused stage kernels (ffe_fused.cu) -------------------------------------
+// One launch advances one SSP-RK3 stage AND applies the E-parallel cleaning
+// of that stage: reads the stage input E,B (set `in`) and, for stages 2-3,
+// the step-start fields (set `en`); writes cleaned E and updated B to `out`.
+struct FusedArgs;
+template <typename R, bool C>
+void launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
+                        int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0, const EB<R>& out,
+                        cudaStream_t st);
+// Tile shape the fused kernel uses (for reporting).
+void fused_tile_shape(int* tx, int* ty);
+
+}  // namespace ffe

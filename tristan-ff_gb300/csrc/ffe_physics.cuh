@@ -1,0 +1,198 @@
+// ffe_physics.cuh — per-cell arithmetic of the force-free update, written once
+// and used by both kernel families:
+//   * the staged kernels (ffe_staged.cu, one launch per reference procedure,
+//     compiled without multiply-add contraction so that they reproduce the
+//     reference's rounding), and
+//   * the fused stage kernels (ffe_fused.cu), which read the same neighbours
+//     from shared-memory tiles.
+// A kernel supplies an accessor `a` with a(F, di, dj, dk) -> value of field F
+// at offset (di, dj, dk) from the current cell and a.rho(di, dj, dk).
+//
+// Every expression keeps the Fortran association of
+// src/algorithms/field_solver.F90 (left to right); line numbers cite that file.
+#pragma once
+#include "ffe_common.cuh"
+
+namespace ffe {
+
+enum { EX = 0, EY, EZ, BX, BY, BZ, B0X, B0Y, B0Z };
+
+template <typename R> __host__ __device__ __forceinline__ R tiny() { return R(1e-7); }
+template <> __host__ __device__ __forceinline__ float tiny<float>() { return 1e-7f; }  // src/defs.F90:4
+
+// rho = div E at offset d (field_solver.F90:57-59)
+template <typename R, class A>
+__device__ __forceinline__ R rho_at(const A& a, int di, int dj, int dk) {
+  return ((a(EX, di, dj, dk) - a(EX, di - 1, dj, dk)) + (a(EY, di, dj, dk) - a(EY, di, dj - 1, dk))) +
+         (a(EZ, di, dj, dk) - a(EZ, di, dj, dk - 1));
+}
+
+// J = CC rho (E x B) / (B^2 + TINY) with the denominator in R, or in double (FP32C).
+template <typename R, bool C>
+__device__ __forceinline__ R jdiv(R cc, R bmag, R bx, R by, R bz, R num) {
+  if (C) {
+    const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
+    return (R)((double)cc / (bd + (double)tiny<float>()) * (double)num);
+  }
+  return cc / (bmag + tiny<R>()) * num;
+}
+
+// rk3Push (field_solver.F90:81-162): writes dE (with -J) and dB of one cell.
+template <typename R, bool C, bool B0, class A>
+__device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
+  const R ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
+  const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
+  d[3] = cc * ((a(EY, 0, 0, 1) - ey0) - (a(EZ, 0, 1, 0) - ez0));
+  d[4] = cc * ((a(EZ, 1, 0, 0) - ez0) - (a(EX, 0, 0, 1) - ex0));
+  d[5] = cc * ((a(EX, 0, 1, 0) - ex0) - (a(EY, 1, 0, 0) - ey0));
+  R cbx = (by0 - a(BY, 0, 0, -1)) - (bz0 - a(BZ, 0, -1, 0));
+  R cby = (bz0 - a(BZ, -1, 0, 0)) - (bx0 - a(BX, 0, 0, -1));
+  R cbz = (bx0 - a(BX, 0, -1, 0)) - (by0 - a(BY, -1, 0, 0));
+  if (B0) {
+    cbx = cbx - ((a(B0Y, 0, 0, 0) - a(B0Y, 0, 0, -1)) - (a(B0Z, 0, 0, 0) - a(B0Z, 0, -1, 0)));
+    cby = cby - ((a(B0Z, 0, 0, 0) - a(B0Z, -1, 0, 0)) - (a(B0X, 0, 0, 0) - a(B0X, 0, 0, -1)));
+    cbz = cbz - ((a(B0X, 0, 0, 0) - a(B0X, 0, -1, 0)) - (a(B0Y, 0, 0, 0) - a(B0Y, -1, 0, 0)));
+  }
+  // -CC * (X) is -(CC*X); the value equals (-CC)*X exactly.
+  d[0] = -(cc * cbx);
+  d[1] = -(cc * cby);
+  d[2] = -(cc * cbz);
+
+  const R r0 = a.rho(0, 0, 0);
+  R intrho, intex, intey, intez, intbx, intby, intbz, bmag, emag;
+  // X current (:91-111)
+  intrho = R(0.5) * (a.rho(1, 0, 0) + r0);
+  intex = ex0;
+  intey = R(0.25) * (((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0));
+  intez = R(0.25) * (((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1));
+  intbx = R(0.125) * (((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
+                        a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1));
+  intby = R(0.5) * (by0 + a(BY, 0, 0, -1));
+  intbz = R(0.5) * (bz0 + a(BZ, 0, -1, 0));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  emag = (intex * intex + intey * intey) + intez * intez;
+  if (emag > bmag) {
+    const R corr = sqrt(bmag / emag);
+    intey = intey * corr;
+    intez = intez * corr;
+  }
+  const R jx = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intey * intbz - intby * intez));
+  // Y current (:114-134)
+  intrho = R(0.5) * (a.rho(0, 1, 0) + r0);
+  intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0));
+  intey = ey0;
+  intez = R(0.25) * (((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1));
+  intbx = R(0.5) * (bx0 + a(BX, 0, 0, -1));
+  intby = R(0.125) * (((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
+                        a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1));
+  intbz = R(0.5) * (bz0 + a(BZ, -1, 0, 0));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  emag = (intex * intex + intey * intey) + intez * intez;
+  if (emag > bmag) {
+    const R corr = sqrt(bmag / emag);
+    intex = intex * corr;
+    intez = intez * corr;
+  }
+  const R jy = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intez * intbx - intex * intbz));
+  // Z current (:137-157)
+  intrho = R(0.5) * (r0 + a.rho(0, 0, 1));
+  intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1));
+  intey = R(0.25) * (((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1));
+  intez = ez0;
+  intbx = R(0.5) * (bx0 + a(BX, 0, -1, 0));
+  intby = R(0.5) * (by0 + a(BY, -1, 0, 0));
+  intbz = R(0.125) * (((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
+                        a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  emag = (intex * intex + intey * intey) + intez * intez;
+  if (emag > bmag) {
+    const R corr = sqrt(bmag / emag);
+    intex = intex * corr;
+    intey = intey * corr;
+  }
+  const R jz = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intex * intby - intbx * intey));
+  d[0] = d[0] - jx;
+  d[1] = d[1] - jy;
+  d[2] = d[2] - jz;
+}
+
+// RK combination (field_solver.F90:187-193): (c1*fn + c2*f) + c3*df, or the
+// FP32C increment form fn + (c2*(f - fn) + c3*df), used when c1 + c2 == 1.
+template <typename R, bool C>
+__device__ __forceinline__ R combine(R c1, R c2, R c3, R fn, R f, R df, bool incr) {
+  if (C && incr) return fn + (c2 * (f - fn) + c3 * df);
+  return (c1 * fn + c2 * f) + c3 * df;
+}
+
+// Absorbing shell (field_solver.F90:210-265) applied to the six updated
+// components of local cell (i, j, k); jg uses i as the reference does (:211).
+template <typename R>
+__device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int jg_i, int kg_i, R v[6]) {
+  const R ig = R(ig_i), jg = R(jg_i), kg = R(kg_i);
+  R r = sqrt(((ig - ab.xc) * (ig - ab.xc) + (jg - ab.yc) * (jg - ab.yc)) + (kg - ab.zc) * (kg - ab.zc));
+  if (!(r > ab.rabsorb - R(1.0))) return;
+  const R h = R(0.5);
+  const R gx[2] = {ig - ab.xc, (ig + h) - ab.xc};
+  const R gy[2] = {jg - ab.yc, (jg + h) - ab.yc};
+  const R gz[2] = {kg - ab.zc, (kg + h) - ab.zc};
+  // staggering of Ex, Ey, Ez, Bx, By, Bz: (1,0,0) (0,1,0) (0,0,1) (0,1,1) (1,0,1) (1,1,0)
+  const int sxo[6] = {1, 0, 0, 0, 1, 1}, syo[6] = {0, 1, 0, 1, 0, 1}, szo[6] = {0, 0, 1, 1, 1, 0};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const R dx = gx[sxo[c]], dy = gy[syo[c]], dz = gz[szo[c]];
+    r = sqrt((dx * dx + dy * dy) + dz * dz);
+    const R dr = (r - ab.rabsorb) / ab.buff;
+    if (dr > R(0.0)) v[c] = (R(1.0) - (dr * dr) * dr) * v[c];
+  }
+}
+
+// cleanEpar (field_solver.F90:288-328): E - (E.B) B / B^2 at the three E points.
+template <typename R, bool C>
+__device__ __forceinline__ R clean_div(R epar, R bi, R bmag, R bx, R by, R bz) {
+  if (C) {
+    const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
+    return (R)((double)(epar * bi) / bd);
+  }
+  return epar * bi / bmag;
+}
+
+template <typename R, bool C, class A>
+__device__ __forceinline__ void clean_cell(const A& a, R e[3]) {
+  const R ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
+  const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
+  R intex, intey, intez, intbx, intby, intbz, bmag, epar;
+  intex = ex0;
+  intey = R(0.25) * (((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0));
+  intez = R(0.25) * (((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1));
+  intbx = R(0.125) * (((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
+                        a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1));
+  intby = R(0.5) * (by0 + a(BY, 0, 0, -1));
+  intbz = R(0.5) * (bz0 + a(BZ, 0, -1, 0));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  epar = (intex * intbx + intey * intby) + intez * intbz;
+  e[0] = ex0 - clean_div<R, C>(epar, intbx, bmag, intbx, intby, intbz);
+
+  intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0));
+  intey = ey0;
+  intez = R(0.25) * (((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1));
+  intbx = R(0.5) * (bx0 + a(BX, 0, 0, -1));
+  intby = R(0.125) * (((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
+                        a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1));
+  intbz = R(0.5) * (bz0 + a(BZ, -1, 0, 0));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  epar = (intex * intbx + intey * intby) + intez * intbz;
+  e[1] = ey0 - clean_div<R, C>(epar, intby, bmag, intbx, intby, intbz);
+
+  intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1));
+  intey = R(0.25) * (((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1));
+  intez = ez0;
+  intbx = R(0.5) * (bx0 + a(BX, 0, -1, 0));
+  intby = R(0.5) * (by0 + a(BY, -1, 0, 0));
+  intbz = R(0.125) * (((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
+                        a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1));
+  bmag = (intbx * intbx + intby * intby) + intbz * intbz;
+  epar = (intex * intbx + intey * intby) + intez * intbz;
+  e[2] = ez0 - clean_div<R, C>(epar, intbz, bmag, intbx, intby, intbz);
+}
+
+}  // namespace ffe

@@ -1,0 +1,292 @@
+"""Python mirror of tristan-ff's field-solver interface over libffe_gb300.so.
+
+The reference's hot path is a set of Fortran module procedures acting on
+module-global arrays (src/algorithms/field_solver.F90, src/tristanmainloop.F90,
+src/logistics/exchange_fields.F90, user/user_*.F90).  `Solver` exposes the same
+procedures, by the same names, on one meshblock resident on one GPU:
+
+    initRKstep()                      field_solver.F90:15
+    rk3Step(c1, c2, c3)               field_solver.F90:35
+    computeRho() / rk3Push() / rk3Update(c1, c2, c3)
+    cleanEpar()                       field_solver.F90:273
+    exchangeFields(exchangeB0=False)  exchange_fields.F90:11
+    userInitialize()                  user_*.F90
+    userFieldBoundaryConditions(step) user_*.F90
+    mainloop(steps, step0)            tristanmainloop.F90:41-84 (step body)
+
+Arrays cross the boundary in the reference's allocation shape: numpy arrays
+of shape (sz+4, sy+4, sx+4) (memory order = Fortran (sx+4, sy+4, sz+4)),
+float64 for FP64 and float32 otherwise.  Every call goes through the C ABI
+(include/ffe.h); there is no CPU fallback: without the library or a GPU the
+constructor raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .inputfile import read_input, desc_from_input  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libffe_gb300.so")
+
+NG = 2
+FP64, FP32, FP32C = 0, 1, 2
+OPEN, PERIODIC, ABSORB = 0, 1, 2
+SETUP_NONE, SETUP_PSR, SETUP_UNIFORM, SETUP_LOOP = 0, 1, 2, 3
+PATH_AUTO, PATH_STAGED, PATH_FUSED, PATH_FUSED_EXACT = 0, 1, 2, 3
+FIELDS = ("ex", "ey", "ez", "bx", "by", "bz", "b0x", "b0y", "b0z",
+          "dex", "dey", "dez", "dbx", "dby", "dbz",
+          "enx", "eny", "enz", "bnx", "bny", "bnz", "rho")
+FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ESTATE",
+          -5: "ENONFINITE", -6: "ETIMEOUT", -7: "EUNSUPPORTED"}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32c": FP32C}
+SETUPS = {"none": SETUP_NONE, "psr": SETUP_PSR, "uniform": SETUP_UNIFORM, "loop": SETUP_LOOP}
+
+# (ex, ey, ez, bx, by, bz) staggering offsets (user/user_psr.F90:54-63, 157-221)
+STAGGER = {"ex": (0.5, 0, 0), "ey": (0, 0.5, 0), "ez": (0, 0, 0.5),
+           "bx": (0, 0.5, 0.5), "by": (0.5, 0, 0.5), "bz": (0.5, 0.5, 0)}
+
+# Exported symbols of the C ABI (kept in step with include/ffe.h).
+ABI_SYMBOLS = (
+    "ffe_abi_version", "ffe_desc_default", "ffe_create", "ffe_destroy", "ffe_last_error",
+    "ffe_field_elems", "ffe_device_bytes", "ffe_upload", "ffe_download",
+    "ffe_init_rk_step", "ffe_compute_rho", "ffe_rk3_push", "ffe_rk3_update", "ffe_rk3_stage",
+    "ffe_clean_epar", "ffe_exchange_fields", "ffe_user_initialize", "ffe_user_bc",
+    "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
+    "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
+)
+
+
+class GridDesc(ctypes.Structure):
+    """ffe_grid_desc of include/ffe.h."""
+    _fields_ = [
+        ("sx", ctypes.c_int32), ("sy", ctypes.c_int32), ("sz", ctypes.c_int32),
+        ("x0", ctypes.c_int32), ("y0", ctypes.c_int32), ("z0", ctypes.c_int32),
+        ("gsx", ctypes.c_int32), ("gsy", ctypes.c_int32), ("gsz", ctypes.c_int32),
+        ("boundary", ctypes.c_int32 * 3),
+        ("absorb_buff", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("setup", ctypes.c_int32),
+        ("path", ctypes.c_int32),
+        ("cc", ctypes.c_double),
+        ("params", ctypes.c_double * 8),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
+def make_desc(size, precision=FP32, boundary=(PERIODIC,) * 3, cc=0.45, absorb_buff=20,
+              setup=SETUP_NONE, params=(), path=PATH_AUTO, offset=(0, 0, 0), gsize=None,
+              stream=None):
+    """Descriptor with the reference's defaults (src/logistics/initialize.F90:139-190)."""
+    sx, sy, sz = size
+    d = GridDesc()
+    d.sx, d.sy, d.sz = sx, sy, sz
+    d.x0, d.y0, d.z0 = offset
+    d.gsx, d.gsy, d.gsz = gsize or size
+    d.boundary[:] = list(boundary)
+    d.absorb_buff = absorb_buff
+    d.precision = PRECISIONS.get(precision, precision) if isinstance(precision, str) else precision
+    d.setup = SETUPS.get(setup, setup) if isinstance(setup, str) else setup
+    d.path = path
+    d.cc = cc
+    p = list(params) + [0.0] * (8 - len(params))
+    d.params[:] = p[:8]
+    d.stream = stream
+    return d
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libffe_gb300.so and declare the C signatures."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FFEError("libffe_gb300.so not built (%s): run tristan-ff_gb300/build.py" % p, -7)
+    lib = ctypes.CDLL(p)
+    H = ctypes.c_void_p
+    i32, dbl, szt = ctypes.c_int32, ctypes.c_double, ctypes.c_size_t
+    sig = {
+        "ffe_abi_version": [],
+        "ffe_desc_default": [ctypes.POINTER(GridDesc), i32, i32, i32],
+        "ffe_create": [ctypes.POINTER(H), ctypes.POINTER(GridDesc)],
+        "ffe_destroy": [H],
+        "ffe_last_error": [H, ctypes.c_char_p, szt],
+        "ffe_field_elems": [H, ctypes.POINTER(szt)],
+        "ffe_device_bytes": [H, ctypes.POINTER(szt)],
+        "ffe_upload": [H, i32, ctypes.c_void_p, szt],
+        "ffe_download": [H, i32, ctypes.c_void_p, szt],
+        "ffe_init_rk_step": [H],
+        "ffe_compute_rho": [H],
+        "ffe_rk3_push": [H],
+        "ffe_rk3_update": [H, dbl, dbl, dbl],
+        "ffe_rk3_stage": [H, dbl, dbl, dbl],
+        "ffe_clean_epar": [H],
+        "ffe_exchange_fields": [H, i32],
+        "ffe_user_initialize": [H],
+        "ffe_user_bc": [H, i32],
+        "ffe_mainloop_prologue": [H],
+        "ffe_step": [H, i32, i32],
+        "ffe_step_path": [H, ctypes.POINTER(i32)],
+        "ffe_step_launches": [H, ctypes.POINTER(i32)],
+        "ffe_check_finite": [H, ctypes.POINTER(i32)],
+        "ffe_synchronize": [H],
+        "ffe_synchronize_timeout": [H, i32],
+        "ffe_init_waves": [H, ctypes.POINTER(ctypes.c_double), i32, ctypes.POINTER(ctypes.c_double)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class FFEError(RuntimeError):
+    def __init__(self, msg, status=None):
+        super().__init__(msg)
+        self.status = status
+
+
+def _last_error(lib, h):
+    buf = ctypes.create_string_buffer(512)
+    lib.ffe_last_error(h, buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+class Solver:
+    """One meshblock on one GPU; method names follow the reference procedures."""
+
+    def __init__(self, desc, lib_path=None):
+        self.lib = load_library(lib_path)
+        self.desc = desc
+        self.h = ctypes.c_void_p()
+        rc = self.lib.ffe_create(ctypes.byref(self.h), ctypes.byref(desc))
+        if rc != 0:
+            raise FFEError("ffe_create: %s (%s)" % (_last_error(self.lib, None), STATUS.get(rc, rc)), rc)
+        self.dtype = np.float64 if desc.precision == FP64 else np.float32
+        self.shape = (desc.sz + 2 * NG, desc.sy + 2 * NG, desc.sx + 2 * NG)
+
+    # -- plumbing ---------------------------------------------------------
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise FFEError("%s: %s (%s)" % (what, _last_error(self.lib, self.h), STATUS.get(rc, rc)), rc)
+
+    def close(self):
+        if self.h:
+            self.lib.ffe_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != self.shape:
+            raise FFEError("upload %s: shape %s, need %s" % (name, a.shape, self.shape), -1)
+        self._ck(self.lib.ffe_upload(self.h, FIELD_ID[name], a.ctypes.data, a.size), "upload " + name)
+
+    def download(self, name):
+        a = np.empty(self.shape, self.dtype)
+        self._ck(self.lib.ffe_download(self.h, FIELD_ID[name], a.ctypes.data, a.size), "download " + name)
+        return a
+
+    def fields(self, names=("ex", "ey", "ez", "bx", "by", "bz")):
+        return {n: self.download(n) for n in names}
+
+    def set_fields(self, d):
+        for n, a in d.items():
+            self.upload(n, a)
+
+    def device_bytes(self):
+        b = ctypes.c_size_t()
+        self._ck(self.lib.ffe_device_bytes(self.h, ctypes.byref(b)), "device_bytes")
+        return b.value
+
+    def step_path(self):
+        p = ctypes.c_int32()
+        self._ck(self.lib.ffe_step_path(self.h, ctypes.byref(p)), "step_path")
+        return p.value
+
+    def step_launches(self):
+        n = ctypes.c_int32()
+        self._ck(self.lib.ffe_step_launches(self.h, ctypes.byref(n)), "step_launches")
+        return n.value
+
+    # -- the reference's procedures ----------------------------------------
+    def initRKstep(self):
+        self._ck(self.lib.ffe_init_rk_step(self.h), "initRKstep")
+
+    def computeRho(self):
+        self._ck(self.lib.ffe_compute_rho(self.h), "computeRho")
+
+    def rk3Push(self):
+        self._ck(self.lib.ffe_rk3_push(self.h), "rk3Push")
+
+    def rk3Update(self, c1, c2, c3):
+        self._ck(self.lib.ffe_rk3_update(self.h, c1, c2, c3), "rk3Update")
+
+    def rk3Step(self, c1, c2, c3):
+        self._ck(self.lib.ffe_rk3_stage(self.h, c1, c2, c3), "rk3Step")
+
+    def cleanEpar(self):
+        self._ck(self.lib.ffe_clean_epar(self.h), "cleanEpar")
+
+    def exchangeFields(self, exchangeB0=False):
+        self._ck(self.lib.ffe_exchange_fields(self.h, 1 if exchangeB0 else 0), "exchangeFields")
+
+    def userInitialize(self):
+        self._ck(self.lib.ffe_user_initialize(self.h), "userInitialize")
+
+    def userFieldBoundaryConditions(self, step):
+        self._ck(self.lib.ffe_user_bc(self.h, step), "userFieldBoundaryConditions")
+
+    def mainloop_prologue(self):
+        self._ck(self.lib.ffe_mainloop_prologue(self.h), "mainloop prologue")
+
+    def mainloop(self, steps, step0=0):
+        """`steps` repetitions of the main-loop body (asynchronous)."""
+        self._ck(self.lib.ffe_step(self.h, steps, step0), "step")
+
+    step = mainloop
+
+    def synchronize(self, timeout_ms=None):
+        if timeout_ms is None:
+            self._ck(self.lib.ffe_synchronize(self.h), "synchronize")
+        else:
+            self._ck(self.lib.ffe_synchronize_timeout(self.h, int(timeout_ms)), "synchronize")
+
+    def init_waves(self, bg, modes):
+        """Synthetic plane-wave workload; modes: array (n, 11), see include/ffe.h."""
+        bgv = (ctypes.c_double * 3)(*[float(x) for x in bg])
+        m = np.ascontiguousarray(np.asarray(modes, np.float64).reshape(-1, 11))
+        self._ck(self.lib.ffe_init_waves(self.h, bgv, m.shape[0],
+                                         m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "init_waves")
+
+    def check_finite(self):
+        ok = ctypes.c_int32()
+        rc = self.lib.ffe_check_finite(self.h, ctypes.byref(ok))
+        if rc not in (0, -5):
+            self._ck(rc, "check_finite")
+        return bool(ok.value)
+
+
+def interior(a):
+    """Interior view [2:-2] on every axis of a ghosted array."""
+    return a[NG:-NG, NG:-NG, NG:-NG]
