@@ -150,7 +150,7 @@ def cpu_baseline(args, edge=None, steps=None, threads=None):
     O.build()
     threads = threads or os.cpu_count() or 1
     edge = edge or args.cpu_sample or 128
-    steps = steps or 2
+    steps = steps or 100
     size = (edge, edge, edge)
     bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
     prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]

@@ -116,6 +116,14 @@ typedef enum {
                               same rounding as FFE_PATH_STAGED, for verification */
 } ffe_path;
 
+/* Opt-in deviation from the reference: clamp the absorbing-shell depth
+   delta_r to 1.  The reference's factor (1 - delta_r^3) of
+   src/algorithms/field_solver.F90:226-263 turns negative and exceeds 1 in
+   magnitude where delta_r > 2^(1/3), which happens in the box corners (the
+   shell is a sphere inscribed in the box), so fields there grow by up to
+   ~100x per stage.  With the clamp the factor stays in [0, 1].            */
+#define FFE_FLAG_ABSORB_CLAMP 1
+
 typedef struct {
   int32_t sx, sy, sz;          /* interior cells of this meshblock           */
   int32_t x0, y0, z0;          /* meshblock corner in the global mesh        */
@@ -125,6 +133,8 @@ typedef struct {
   int32_t precision;           /* ffe_precision                              */
   int32_t setup;               /* ffe_setup                                  */
   int32_t path;                /* ffe_path                                   */
+  int32_t flags;               /* FFE_FLAG_* bits, 0 = the reference's behaviour */
+  int32_t reserved;            /* must be 0                                  */
   double cc;                   /* <algorithm> c, the Courant number          */
   double params[FFE_MAX_PARAMS];
   void* stream;                /* cudaStream_t to order work on, or NULL     */

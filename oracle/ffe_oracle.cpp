@@ -58,6 +58,7 @@ struct Desc {
   int absorb_buff;
   int precision;  // 0 fp64, 1 fp32, 2 fp32c
   int setup;      // 0 none, 1 psr, 2 uniform, 3 loop
+  int flags;      // 1: clamp the absorbing depth to 1 (this library's opt-in)
   double cc;
   double params[8];
 };
@@ -327,7 +328,8 @@ struct Oracle : OracleBase {
           const R dy = oy[c] != R(0) ? (jg + oy[c]) - yc : jg - yc;
           const R dz = oz[c] != R(0) ? (kg + oz[c]) - zc : kg - zc;
           r = std::sqrt((dx * dx + dy * dy) + dz * dz);
-          const R delta_r = (r - rabsorb) / buff;
+          R delta_r = (r - rabsorb) / buff;
+          if ((d.flags & 1) && delta_r > R(1.0)) delta_r = R(1.0);
           if (delta_r > R(0.0)) f[c][s] = (R(1.0) - (delta_r * delta_r) * delta_r) * f[c][s];
         }
       }
@@ -722,7 +724,7 @@ extern "C" {
 typedef struct {
   int32_t sx, sy, sz, x0, y0, z0, gsx, gsy, gsz;
   int32_t boundary[3];
-  int32_t absorb_buff, precision, setup, path;
+  int32_t absorb_buff, precision, setup, path, flags, reserved;
   double cc;
   double params[8];
   void* stream;
@@ -738,6 +740,7 @@ void* ora_create(const ora_desc* in) {
   d.absorb_buff = in->absorb_buff;
   d.precision = in->precision;
   d.setup = in->setup;
+  d.flags = in->flags;
   d.cc = in->cc;
   for (int i = 0; i < 8; ++i) d.params[i] = in->params[i];
   if (d.sx < NG || d.sy < NG || d.sz < NG) {

@@ -44,11 +44,11 @@ def test_abi_version_and_descriptor_defaults(lib):
 
 
 def test_descriptor_layout_matches_header():
-    # int32 x 16, then double cc at offset 64, params, stream pointer
-    assert ffe.GridDesc.cc.offset == 64
-    assert ffe.GridDesc.params.offset == 72
-    assert ffe.GridDesc.stream.offset == 136
-    assert ctypes.sizeof(ffe.GridDesc) == 144
+    # int32 x 18, then double cc at offset 72, params, stream pointer
+    assert ffe.GridDesc.cc.offset == 72
+    assert ffe.GridDesc.params.offset == 80
+    assert ffe.GridDesc.stream.offset == 144
+    assert ctypes.sizeof(ffe.GridDesc) == 152
 
 
 def test_create_rejects_bad_descriptors_without_a_gpu(lib):

@@ -145,6 +145,7 @@ template <typename R> Absorb<R> absorb_consts(ffe_t h) {
   const R rmax = std::min(std::min(a.xc, a.yc), a.zc);
   a.rabsorb = rmax - R(h->p.absorb_buff);
   a.buff = R(h->p.absorb_buff);
+  a.clamp = (h->d.flags & FFE_FLAG_ABSORB_CLAMP) ? 1 : 0;
   return a;
 }
 
@@ -322,7 +323,16 @@ int step_staged(ffe_t h, int nsteps, int step0) {
   return FFE_OK;
 }
 
-bool fused_possible(ffe_t h) { return h->d.setup == FFE_SETUP_NONE; }
+// The fused kernels compute halo cells on a periodic face from the arrays'
+// ghost values.  With mixed periodic/open axes, ghost cells that lie outside
+// both kinds of face keep frozen values that are not periodic images, so the
+// image of a cell next to an open face can differ: those grids run staged.
+bool fused_possible(ffe_t h) {
+  const int* b = h->d.boundary;
+  const bool all_per = b[0] == 1 && b[1] == 1 && b[2] == 1;
+  const bool none_per = b[0] != 1 && b[1] != 1 && b[2] != 1;
+  return h->d.setup == FFE_SETUP_NONE && (all_per || none_per);
+}
 
 template <typename R>
 int sync_ghosts(ffe_t h) {
@@ -369,7 +379,7 @@ int do_step(ffe_t h, int nsteps, int step0) {
   const int path = h->d.path;
   if (path == FFE_PATH_STAGED || (path == FFE_PATH_AUTO && !fused_possible(h))) return step_staged<R, C>(h, nsteps, step0);
   if (!fused_possible(h))
-    return fail(h, FFE_EUNSUPPORTED, "fused path needs setup NONE (user boundary conditions run staged)");
+    return fail(h, FFE_EUNSUPPORTED, "fused path needs setup NONE and all-periodic or all-non-periodic boundaries");
   return step_fused<R, C>(h, nsteps, path == FFE_PATH_FUSED_EXACT);
 }
 
@@ -418,6 +428,7 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   if (d.precision < FFE_FP64 || d.precision > FFE_FP32C) return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
   if (d.setup < FFE_SETUP_NONE || d.setup > FFE_SETUP_LOOP) return set_thread_err(FFE_EINVAL, "bad setup %d", d.setup);
   if (d.path < FFE_PATH_AUTO || d.path > FFE_PATH_FUSED_EXACT) return set_thread_err(FFE_EINVAL, "bad path %d", d.path);
+  if ((d.flags & ~FFE_FLAG_ABSORB_CLAMP) || d.reserved) return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
   for (int a = 0; a < 3; ++a)
     if (d.boundary[a] < 0 || d.boundary[a] > 2) return set_thread_err(FFE_EINVAL, "bad boundary %d", d.boundary[a]);
   // one absorbing axis makes all three absorbing (src/logistics/initialize.F90:144-148)

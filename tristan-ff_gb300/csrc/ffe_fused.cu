@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(NT) k_fused(const Params<R> P) {
   load_old(kb + 1);
   __syncthreads();
   compute_new(kb);
+  __syncthreads();  // compute_new(kb) reads OLD(kb-1), whose slot load_old(kb+2) reuses
   for (int k = kb; k < ke; ++k) {
     load_old(k + 2);
     __syncthreads();

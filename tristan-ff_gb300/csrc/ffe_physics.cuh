@@ -141,7 +141,8 @@ __device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int j
   for (int c = 0; c < 6; ++c) {
     const R dx = gx[sxo[c]], dy = gy[syo[c]], dz = gz[szo[c]];
     r = sqrt((dx * dx + dy * dy) + dz * dz);
-    const R dr = (r - ab.rabsorb) / ab.buff;
+    R dr = (r - ab.rabsorb) / ab.buff;
+    if (ab.clamp && dr > R(1.0)) dr = R(1.0);
     if (dr > R(0.0)) v[c] = (R(1.0) - (dr * dr) * dr) * v[c];
   }
 }

@@ -36,6 +36,7 @@ FP64, FP32, FP32C = 0, 1, 2
 OPEN, PERIODIC, ABSORB = 0, 1, 2
 SETUP_NONE, SETUP_PSR, SETUP_UNIFORM, SETUP_LOOP = 0, 1, 2, 3
 PATH_AUTO, PATH_STAGED, PATH_FUSED, PATH_FUSED_EXACT = 0, 1, 2, 3
+FLAG_ABSORB_CLAMP = 1
 FIELDS = ("ex", "ey", "ez", "bx", "by", "bz", "b0x", "b0y", "b0z",
           "dex", "dey", "dez", "dbx", "dby", "dbz",
           "enx", "eny", "enz", "bnx", "bny", "bnz", "rho")
@@ -71,6 +72,8 @@ class GridDesc(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("setup", ctypes.c_int32),
         ("path", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("cc", ctypes.c_double),
         ("params", ctypes.c_double * 8),
         ("stream", ctypes.c_void_p),
@@ -79,7 +82,7 @@ class GridDesc(ctypes.Structure):
 
 def make_desc(size, precision=FP32, boundary=(PERIODIC,) * 3, cc=0.45, absorb_buff=20,
               setup=SETUP_NONE, params=(), path=PATH_AUTO, offset=(0, 0, 0), gsize=None,
-              stream=None):
+              stream=None, flags=0):
     """Descriptor with the reference's defaults (src/logistics/initialize.F90:139-190)."""
     sx, sy, sz = size
     d = GridDesc()
@@ -91,6 +94,7 @@ def make_desc(size, precision=FP32, boundary=(PERIODIC,) * 3, cc=0.45, absorb_bu
     d.precision = PRECISIONS.get(precision, precision) if isinstance(precision, str) else precision
     d.setup = SETUPS.get(setup, setup) if isinstance(setup, str) else setup
     d.path = path
+    d.flags = flags
     d.cc = cc
     p = list(params) + [0.0] * (8 - len(params))
     d.params[:] = p[:8]

@@ -64,17 +64,21 @@ def host_waves(size, bg, modes, dtype=np.float64):
     """The same fields computed with numpy (ghosted arrays), for small grids."""
     sx, sy, sz = size
     ng = 2
-    k, j, i = np.meshgrid(np.arange(-ng, sz + ng), np.arange(-ng, sy + ng), np.arange(-ng, sx + ng),
-                          indexing="ij")
+    i = np.arange(-ng, sx + ng, dtype=np.float64)[None, None, :]
+    j = np.arange(-ng, sy + ng, dtype=np.float64)[None, :, None]
+    k = np.arange(-ng, sz + ng, dtype=np.float64)[:, None, None]
+    shape = (sz + 2 * ng, sy + 2 * ng, sx + 2 * ng)
     offs = {"ex": (0.5, 0, 0), "ey": (0, 0.5, 0), "ez": (0, 0, 0.5),
             "bx": (0, 0.5, 0.5), "by": (0.5, 0, 0.5), "bz": (0.5, 0.5, 0)}
     out = {}
     for c, name in enumerate(("ex", "ey", "ez", "bx", "by", "bz")):
         ox, oy, oz = offs[name]
-        v = np.full(i.shape, bg[c - 3] if c >= 3 else 0.0)
+        v = np.full(shape, bg[c - 3] if c >= 3 else 0.0)
         for m in modes:
             K, phi, a, u, n = m[0:3], m[3], m[4], m[5:8], m[8:11]
-            s = np.sin(K[0] * (i + ox) + K[1] * (j + oy) + K[2] * (k + oz) + phi)
+            # sin of a sum of separable phases, through complex exponentials
+            s = (np.exp(1j * (K[2] * (k + oz) + phi)) * np.exp(1j * K[1] * (j + oy)) *
+                 np.exp(1j * K[0] * (i + ox))).imag
             db = [-a * s * u[0], -a * s * u[1], -a * s * u[2]]
             if c < 3:
                 cr = [n[1] * db[2] - n[2] * db[1], n[2] * db[0] - n[0] * db[2], n[0] * db[1] - n[1] * db[0]]
