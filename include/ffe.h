@@ -123,6 +123,12 @@ typedef enum {
    shell is a sphere inscribed in the box), so fields there grow by up to
    ~100x per stage.  With the clamp the factor stays in [0, 1].            */
 #define FFE_FLAG_ABSORB_CLAMP 1
+/* Opt-in deviation: add TINY to the B^2 denominators of cleanEpar, as the
+   reference does for the current (field_solver.F90:111) but not for the
+   cleaning (:300,314,328), where B = 0 gives 0/0 = NaN.  An absorbing shell
+   drives B to zero at the box corners, so a run with FFE_FLAG_ABSORB_CLAMP
+   needs this flag to stay finite.                                          */
+#define FFE_FLAG_CLEAN_TINY 2
 
 typedef struct {
   int32_t sx, sy, sz;          /* interior cells of this meshblock           */

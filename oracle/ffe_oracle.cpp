@@ -109,6 +109,7 @@ struct Oracle : OracleBase {
     for (int f = 0; f < F_N; ++f) a[f].assign(ntot, R(0));
     CC = R(d.cc);
     CCINV = R(1.0) / CC;  // src/logistics/initialize.F90:190
+    if (d.flags & 2) ct = TINYR();
     setup_constants();
   }
 
@@ -337,13 +338,15 @@ struct Oracle : OracleBase {
   }
 
   // ---- cleanEpar: field_solver.F90:273-335 ------------------------------
-  static inline R clean_term(R epar, R bi, R bmag, R intbx, R intby, R intbz) {
+  // ct = 0 as in the reference, or TINY under this library's opt-in flag 2
+  R ct = R(0);
+  inline R clean_term(R epar, R bi, R bmag, R intbx, R intby, R intbz) const {
     if (COMP) {
       double bd = ((double)intbx * (double)intbx + (double)intby * (double)intby) +
                   (double)intbz * (double)intbz;
-      return (R)((double)(epar * bi) / bd);
+      return (R)((double)(epar * bi) / (bd + (double)ct));
     }
-    return epar * bi / bmag;
+    return epar * bi / (bmag + ct);
   }
 
   void clean() override {

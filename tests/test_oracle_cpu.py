@@ -233,3 +233,25 @@ def test_uniform_bc_sets_the_footpoint_twist(oracle_mod):
     ex = o.download("ex")
     assert np.any(ex[0:3] != 0)            # planes z <= 0 are driven
     assert np.all(ex[3:-2] == 0)           # interior untouched
+
+
+def test_absorbing_corners_amplify_unless_clamped(oracle_mod):
+    """field_solver.F90:226-263: (1 - dr^3) < -1 in the box corners, so the
+    reference's shell amplifies there; the opt-in clamp + cleaning TINY keep a
+    pulsar run finite and damp the corners."""
+    size = (24, 24, 24)
+    prm = (4.0, 30.0, 100.0, 1.0)
+    peak = {}
+    for flags in (0, ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY):
+        d = ffe.make_desc(size, precision=ffe.FP64, boundary=(2, 2, 2), absorb_buff=4,
+                          setup=ffe.SETUP_PSR, params=prm, flags=flags)
+        o = oracle_mod.Oracle(d)
+        o.userInitialize()
+        o.mainloop_prologue()
+        o.mainloop(6, 0)
+        bx = ffe.interior(o.download("bx"))
+        corner = np.abs(bx[0, :, 0])            # i = 0, k = 0 line: the largest dr
+        peak[flags] = np.nanmax(corner) if np.isfinite(corner).any() else np.inf
+        if flags:
+            assert np.all(np.isfinite(bx))
+    assert peak[0] > 1e3 * peak[ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY]

@@ -22,15 +22,9 @@
 #include <thread>
 #include <string>
 #include <new>
+#include <cuda.h>
 #include "../../include/ffe.h"
 #include "ffe_kernels.h"
-
-namespace ffe {
-template <typename R, bool C>
-void launch_fused_stage_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
-                              int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0,
-                              const EB<R>& out, cudaStream_t st);
-}
 
 using namespace ffe;
 
@@ -71,7 +65,11 @@ struct ffe_solver {
   void* box = nullptr;
   size_t box_bytes = 0;
   void* param = nullptr;  // device copy of the wave-mode table
-  int* dflag = nullptr;
+  int* dflag = nullptr;   // finite-check word
+  int* derr = nullptr;    // fused-kernel timeout word
+  bool maps_ok = false;   // TMA tensor maps encoded
+  CUtensorMap tm_old[3][6];  // per field array: box of tile + 2 halo (stage input)
+  CUtensorMap tm_en[3][6];   // per field array: box of tile + 1 halo rows (step start)
   int cur = 0;
   bool has_b0 = false;
   bool ghosts_synced = false;  // all three sets hold the same ghost values
@@ -147,6 +145,11 @@ template <typename R> Absorb<R> absorb_consts(ffe_t h) {
   a.buff = R(h->p.absorb_buff);
   a.clamp = (h->d.flags & FFE_FLAG_ABSORB_CLAMP) ? 1 : 0;
   return a;
+}
+
+// TINY added to the cleaning denominators only under FFE_FLAG_CLEAN_TINY.
+template <typename R> R clean_tiny(ffe_t h) {
+  return (h->d.flags & FFE_FLAG_CLEAN_TINY) ? (sizeof(R) == 4 ? R(1e-7f) : R(1e-7)) : R(0);
 }
 
 // user/user_psr.F90:26-37 and :345-374, evaluated in R on the host.
@@ -231,7 +234,7 @@ int op_update(ffe_t h, double c1, double c2, double c3) {
 
 template <typename R, bool C>
 int op_clean(ffe_t h) {
-  launch_clean<R, C>(h->g, eb_of<R>(h, h->cur), eb_of<R>(h, s_d(h)), h->st);
+  launch_clean<R, C>(h->g, eb_of<R>(h, h->cur), eb_of<R>(h, s_d(h)), clean_tiny<R>(h), h->st);
   return check_launch(h, "cleanEpar");
 }
 
@@ -331,7 +334,7 @@ bool fused_possible(ffe_t h) {
   const int* b = h->d.boundary;
   const bool all_per = b[0] == 1 && b[1] == 1 && b[2] == 1;
   const bool none_per = b[0] != 1 && b[1] != 1 && b[2] != 1;
-  return h->d.setup == FFE_SETUP_NONE && (all_per || none_per);
+  return h->d.setup == FFE_SETUP_NONE && (all_per || none_per) && h->maps_ok;
 }
 
 template <typename R>
@@ -360,13 +363,17 @@ int step_fused(ffe_t h, int nsteps, bool exact) {
       double c[3];
       stage_coeffs<R>(s, c);
       const bool incr = C && std::fabs(c[0] + c[1] - 1.0) < 1e-12;
+      const void* mi = h->tm_old[ins[s]];
+      const void* me = h->tm_en[A];
+      int lr;
       if (exact)
-        launch_fused_stage_exact<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1,
-                                       ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
-                                       h->st);
+        lr = launch_fused_stage_exact<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi,
+                                            me, b0, h->has_b0, eb_of<R>(h, outs[s]), clean_tiny<R>(h), h->derr,
+                                            h->st);
       else
-        launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1,
-                                 ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]), h->st);
+        lr = launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi, me,
+                                      b0, h->has_b0, eb_of<R>(h, outs[s]), clean_tiny<R>(h), h->derr, h->st);
+      if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
       if ((rc = check_launch(h, "fused stage"))) return rc;
     }
     h->cur = B;
@@ -428,7 +435,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   if (d.precision < FFE_FP64 || d.precision > FFE_FP32C) return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
   if (d.setup < FFE_SETUP_NONE || d.setup > FFE_SETUP_LOOP) return set_thread_err(FFE_EINVAL, "bad setup %d", d.setup);
   if (d.path < FFE_PATH_AUTO || d.path > FFE_PATH_FUSED_EXACT) return set_thread_err(FFE_EINVAL, "bad path %d", d.path);
-  if ((d.flags & ~FFE_FLAG_ABSORB_CLAMP) || d.reserved) return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
+  if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY)) || d.reserved)
+    return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
   for (int a = 0; a < 3; ++a)
     if (d.boundary[a] < 0 || d.boundary[a] > 2) return set_thread_err(FFE_EINVAL, "bad boundary %d", d.boundary[a]);
   // one absorbing axis makes all three absorbing (src/logistics/initialize.F90:144-148)
@@ -516,6 +524,7 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   h->param = base + off;
   off += pbytes;
   h->dflag = (int*)(base + off);
+  h->derr = h->dflag + 1;
   e = cudaMemsetAsync(h->arena, 0, total, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) {
@@ -523,6 +532,17 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
     if (h->own_stream) cudaStreamDestroy(h->st);
     delete h;
     return set_thread_err(FFE_ECUDA, "arena clear: %s", cudaGetErrorString(e));
+  }
+  // TMA tensor maps of every field array for the fused kernels
+  h->maps_ok = true;
+  for (int s = 0; s < 3 && h->maps_ok; ++s)
+    for (int c = 0; c < 6 && h->maps_ok; ++c)
+      h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es) == 0;
+  if (!h->maps_ok && d.path >= FFE_PATH_FUSED) {
+    cudaFree(h->arena);
+    if (h->own_stream) cudaStreamDestroy(h->st);
+    delete h;
+    return set_thread_err(FFE_EUNSUPPORTED, "cannot encode TMA tensor maps for the fused path");
   }
   *out = h;
   return FFE_OK;
@@ -717,11 +737,24 @@ int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* mo
   return check_launch(h, "init_waves");
 }
 
+// A fused-stage block that gave up waiting for its TMA copies leaves a 1 in
+// the handle's error word; report it (and clear it) once the stream is idle.
+static int check_device_error(ffe_t h) {
+  int e = 0;
+  FFE_CUDA(h, cudaMemcpyAsync(&e, h->derr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  FFE_CUDA(h, cudaStreamSynchronize(h->st));
+  if (e) {
+    FFE_CUDA(h, cudaMemsetAsync(h->derr, 0, sizeof(int), h->st));
+    return fail(h, FFE_ETIMEOUT, "a fused-stage block timed out waiting for its plane copies");
+  }
+  return FFE_OK;
+}
+
 int ffe_synchronize(ffe_t h) {
   int rc;
   if ((rc = check_handle(h))) return rc;
   FFE_CUDA(h, cudaStreamSynchronize(h->st));
-  return FFE_OK;
+  return check_device_error(h);
 }
 
 int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms) {
@@ -730,7 +763,7 @@ int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms) {
   const auto t0 = std::chrono::steady_clock::now();
   for (;;) {
     cudaError_t e = cudaStreamQuery(h->st);
-    if (e == cudaSuccess) return FFE_OK;
+    if (e == cudaSuccess) return check_device_error(h);
     if (e != cudaErrorNotReady) return fail(h, FFE_ECUDA, "cudaStreamQuery: %s", cudaGetErrorString(e));
     const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
     if (ms >= timeout_ms) return fail(h, FFE_ETIMEOUT, "stream not idle after %d ms", timeout_ms);

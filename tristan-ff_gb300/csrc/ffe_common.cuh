@@ -4,12 +4,15 @@
 //   * index (i, j, k) with i, j, k in [-2, s+1] (NGHOST = 2, as the reference's
 //     allocation, src/logistics/initialize.F90:192-199), x fastest;
 //   * each x-row is padded to a pitch of px elements (a multiple of 128 bytes)
-//     and cell i = 0 sits at element OX of its row, so that every interior row
-//     starts on a 16-byte boundary (OX = 4 floats or 2 doubles; the two ghost
-//     cells sit just before it);
+//     and cell i = 0 sits at element OX = 2 of its row, so that ghost cell
+//     i = -2 starts the row: a tile whose first cell is x0 - 2 (x0 a multiple
+//     of 32) then starts on a 128-byte boundary, as TMA boxes must;
 //   * rows per plane py = sy + 4, planes sz + 4.
 // A reference-layout host array (sx+4 contiguous values per row) maps onto this
 // with one pitched 2-D copy (ffe_api.cu).
+//
+// Since a row holds cells -2 .. s+1 from element 0, the TMA tensor coordinate of
+// cell (i, j, k) is (i + 2, j + 2, k + 2).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,7 +22,7 @@ namespace ffe {
 constexpr int NG = 2;
 
 template <typename R> struct Layout;
-template <> struct Layout<float> { static constexpr int OX = 4; static constexpr int PXA = 32; };
+template <> struct Layout<float> { static constexpr int OX = 2; static constexpr int PXA = 32; };
 template <> struct Layout<double> { static constexpr int OX = 2; static constexpr int PXA = 16; };
 
 struct Geom {

@@ -1,43 +1,82 @@
 // ffe_fused.cu — one launch per SSP-RK3 stage: computeRho + rk3Push +
 // rk3Update (+ absorbing shell) + ghost fill + cleanEpar + ghost fill.
 //
-// Data flow of one launch (block = TX x TY column of cells, marching in z
-// through a chunk of planes):
-//   OLD ring   : stage-input E,B on 3 planes over the tile + 2 halo cells
-//   NEW ring   : updated (not yet cleaned) E,B on 3 planes over tile + 1 halo
-//   per plane k: load OLD(k+2); compute NEW(k+1) on tile+1 (push + update);
-//                clean plane k on the tile from NEW(k-1..k+1); store.
-// The halo-1 ring of NEW is recomputed by neighbouring blocks (1.33x push
-// work for a 32x8 tile) instead of a second pass over memory, so a stage
-// reads E,B (+ step-start E,B for stages 2-3) once and writes E,B once.
+// A block owns a TX x TY column of cells and marches in z through a chunk of
+// planes.  Shared memory holds three plane rings:
+//   OLD (depth 5): stage-input E,B over the tile + 2 halo cells, one TMA box
+//                  per component and plane, fetched two planes ahead;
+//   EN  (depth 2): step-start E,B over the tile + 1 halo (stages 2 and 3),
+//                  fetched one plane ahead;
+//   NEW (depth 4): updated, not yet cleaned E,B over the tile + 1 halo.
+// Per plane k:  thread 0 issues TMA for OLD(k+3..k+4), EN(k+2);
+//               wait OLD(k+2), EN(k+1) -> NEW(k+1) = push + update on
+//               tile+1 (one thread per cell of the 34 x 10 region) ->
+//               barrier -> clean plane k on the tile from NEW(k-1..k+1),
+//               store E'' and B'.
+// With four NEW slots the clean of plane k and the push of plane k+2 touch
+// different slots, so one barrier per plane suffices and warps that have no
+// clean work move on to the next push.  A stage reads E,B (and the
+// step-start E,B for stages 2-3) once from HBM and writes E,B once; the halo
+// ring of NEW (1.33x the push work of a 32x8 tile) is recomputed instead of
+// making a second pass over memory.
 //
 // Ghosts.  The reference refreshes ghosts by exchangeFields after the update
 // and after the cleaning (src/tristanmainloop.F90:59-61).  Here a cell lying
-// within 2 cells of a periodic face is also stored at its periodic image in
+// within 2 cells of a periodic face is also stored at its periodic images in
 // the ghost shell, so the output arrays leave the kernel with valid ghosts
 // and the next stage reads plain indices.  On open / absorbing axes ghosts
 // keep the values they were given at set-up (no neighbour sends them,
-// src/tools/helpers.F90:27-45), and the halo cells of NEW that lie there take
-// those frozen values.
+// src/tools/helpers.F90:27-45), and NEW takes those frozen values there.
 //
-// Compiled twice: normally (multiply-add contraction on; the fast path) and
-// with -fmad=false under FFE_FUSED_EXACT (bit-comparable with the oracle).
+// Waits on the TMA barriers are bounded: a block that gives up sets the error
+// word (read by ffe_synchronize as FFE_ETIMEOUT), drains its copies in flight
+// with bounded waits and returns.
+//
+// Compiled twice: normally (multiply-add contraction and, in FP32, the
+// reciprocal-multiply quotient) as the fast path, and with -fmad=false under
+// FFE_FUSED_EXACT with correctly rounded division (bit-comparable with the
+// oracle).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstring>
 #include "ffe_kernels.h"
 #include "ffe_physics.cuh"
 
 #ifdef FFE_FUSED_EXACT
 #define FFE_FUSED_NS fused_exact
+#define FFE_FAST false
 #else
 #define FFE_FUSED_NS fused_fast
+#define FFE_FAST true
 #endif
 
 namespace ffe {
 namespace FFE_FUSED_NS {
 
 constexpr int TX = 32, TY = 8;
-constexpr int HX = TX + 4, HY = TY + 4;  // OLD tile incl. 2 halo
-constexpr int NX = TX + 2, NY = TY + 2;  // NEW tile incl. 1 halo
-constexpr int NT = TX * TY;
+constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+TX+1)
+constexpr int OH = TY + 4;               // OLD box rows (y0-2 .. y0+TY+1)
+constexpr int EH = TY + 2;               // EN box rows (y0-1 .. y0+TY)
+constexpr int NX = TX + 2, NY = TY + 2;  // NEW tile (tile + 1 halo)
+constexpr int NCELL = NX * NY;           // 340
+constexpr int NT = (NCELL + 31) / 32 * 32;  // 352 threads: one per NEW cell
+constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
+constexpr long long WAIT_LIMIT = 1LL << 22;
+
+template <typename R> struct Sizes {
+  static constexpr int OLDBOX = ((OW * OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);  // elements
+  static constexpr int ENBOX = ((OW * EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
+  static constexpr int NEWPL = NY * NX;  // one component of one NEW plane
+  static constexpr int OLD = DO * 6 * OLDBOX;
+  static constexpr int EN = DE * 6 * ENBOX;
+  static constexpr int NEW = DN * 6 * NEWPL;
+  static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * (DO + DE);
+};
+
+struct Maps {  // one 3-D tensor map per component: stage input (OLD) and step start (EN)
+  CUtensorMap in[6];
+  CUtensorMap en[6];
+};
 
 template <typename R>
 struct Params {
@@ -45,130 +84,219 @@ struct Params {
   Phys p;
   Absorb<R> ab;
   R cc, c1, c2, c3;
+  R ct;  // TINY in the cleaning denominator (opt-in), else 0
   int incr;
-  int kz;               // planes per block
-  const R* in[6];
-  const R* en[6];
+  int kz;  // planes per block
   const R* b0[3];
   R* out[6];
+  int* err;
 };
 
+// ---- PTX helpers: mbarrier + TMA ------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: true when the phase completed
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (long long it = 0; it < WAIT_LIMIT; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map, int x, int y, int z, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// Accessor over the OLD ring for push_cell: b[dk+1] points at this thread's
+// cell in plane p+dk, so every (component, di, dj) offset is a constant.
 template <typename R>
-struct SmemOld {  // accessor over the OLD ring for push_cell
-  const R* old;   // [3][6][HY][HX]
+struct SmemOld {
+  const R* b[3];
   const R* const* b0;
   long long gs, dj, dk;  // global index of the cell (for B0)
-  int x, y;              // local position in OLD coordinates
-  int s[3];              // ring slot of plane offset -1, 0, +1
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
     if (c >= 6) return __ldg(b0[c - 6] + gs + di + djj * dj + dkk * dk);
-    return old[((s[dkk + 1] * 6 + c) * HY + (y + djj)) * HX + (x + di)];
+    return b[dkk + 1][c * Sizes<R>::OLDBOX + djj * OW + di];
   }
   __device__ __forceinline__ R rho(int di, int djj, int dkk) const { return rho_at<R>(*this, di, djj, dkk); }
 };
 
+// Accessor over the NEW ring for clean_cell.
 template <typename R>
-struct SmemNew {  // accessor over the NEW ring for clean_cell
-  const R* nw;    // [3][6][NY][NX]
-  int x, y;
-  int s[3];
+struct SmemNew {
+  const R* b[3];
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
-    return nw[((s[dkk + 1] * 6 + c) * NY + (y + djj)) * NX + (x + di)];
+    return b[dkk + 1][c * Sizes<R>::NEWPL + djj * NX + di];
   }
 };
 
-__device__ __forceinline__ int slot(int p) { return (p + 3000) % 3; }
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
 template <typename R, bool C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(NT) k_fused(const Params<R> P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R* old = reinterpret_cast<R*>(smem_raw);  // 3*6*HY*HX
-  R* nw = old + 3 * 6 * HY * HX;            // 3*6*NY*NX
+__global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
+  using S = Sizes<R>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  R* old = reinterpret_cast<R*>(smem_raw);
+  R* en = old + S::OLD;
+  R* nw = en + S::EN;
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(nw + S::NEW);
   const Geom& g = P.g;
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int kb = blockIdx.z * P.kz;
   const int ke = min(kb + P.kz, g.sz);
   const bool per_x = P.p.bnd[0] == 1, per_y = P.p.bnd[1] == 1, per_z = P.p.bnd[2] == 1;
+  constexpr bool FD = FFE_FAST && !C && sizeof(R) == 4;
 
-  auto load_old = [&](int p) {
-    const int sl = slot(p);
-    const int pz = clampi(p, -NG, g.sz + NG - 1);
-    for (int e = tid; e < HX * HY; e += NT) {
-      const int lx = e % HX, ly = e / HX;
-      const int gi = clampi(x0 - 2 + lx, -NG, g.sx + NG - 1);
-      const int gj = clampi(y0 - 2 + ly, -NG, g.sy + NG - 1);
-      const long long gidx = g.idx(gi, gj, pz);
+  const unsigned bar_old = smem_u32(bars), bar_en = smem_u32(bars + DO);
+  // plane p of OLD is use m = p - (kb-2) of slot m % DO; EN: m = p - (kb-1), slot m % DE
+  auto old_slot = [&](int p) { return (p - (kb - 2)) % DO; };
+  auto old_par = [&](int p) { return (unsigned)(((p - (kb - 2)) / DO) & 1); };
+  auto en_slot = [&](int p) { return (p - (kb - 1)) % DE; };
+  auto en_par = [&](int p) { return (unsigned)(((p - (kb - 1)) / DE) & 1); };
+  auto new_slot = [&](int p) { return (p - (kb - 1)) % DN; };
+
+  auto issue_old = [&](int p) {  // one thread
+    const int s = old_slot(p);
+    const unsigned bar = bar_old + 8 * s;
+    mbar_expect_tx(bar, 6u * OW * OH * sizeof(R));
 #pragma unroll
-      for (int c = 0; c < 6; ++c) old[((sl * 6 + c) * HY + ly) * HX + lx] = P.in[c][gidx];
-    }
+    for (int c = 0; c < 6; ++c)
+      tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), &maps.in[c], x0, y0, p + NG, bar);
   };
+  auto issue_en = [&](int p) {
+    const int s = en_slot(p);
+    const unsigned bar = bar_en + 8 * s;
+    mbar_expect_tx(bar, 6u * OW * EH * sizeof(R));
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+      tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), &maps.en[c], x0, y0 + 1, p + NG, bar);
+  };
+
+  if (tid == 0) {
+    for (int s = 0; s < DO + DE; ++s) mbar_init(smem_u32(bars + s), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb (never past the last plane used)
+  int old_next = kb - 2, en_next = kb - 1;
+  const int old_last = ke + 1, en_last = ke;
+  if (tid == 0) {
+    for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
+    if (!STAGE1)
+      for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
+  }
+  // At the top of iteration k, every thread has finished compute_new(k): the
+  // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
+  // may run to k+4 and EN to k+2.
+  auto refill = [&](int k) {
+    if (tid != 0) return;
+    while (old_next <= old_last && old_next <= k + 4) issue_old(old_next++);
+    if (!STAGE1)
+      while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
+  };
+  auto wait_planes = [&](int p_old, int p_en) {
+    bool ok = mbar_wait(bar_old + 8 * old_slot(p_old), old_par(p_old));
+    if (!STAGE1) ok = ok && mbar_wait(bar_en + 8 * en_slot(p_en), en_par(p_en));
+    return ok;
+  };
+
+  // ---- per-thread constants --------------------------------------------------
+  const int nxl = tid % NX, nyl = tid / NX;  // NEW cell of this thread (tid < NCELL)
+  const int gi = x0 - 1 + nxl, gj = y0 - 1 + nyl;
+  const bool xy_in = tid < NCELL && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
+  const bool out_xy_open = ((gi < 0 || gi >= g.sx) && !per_x) || ((gj < 0 || gj >= g.sy) && !per_y);
+  const int toff_old = (nyl + 1) * OW + (nxl + 1);  // this cell in an OLD box
+  const int toff_en = nyl * OW + (nxl + 1);         // in an EN box
+  const int toff_new = nyl * NX + nxl;              // in a NEW plane
+  long long gbase = 0;
+  if (B0 && xy_in) gbase = g.idx(gi, gj, 0);
 
   auto compute_new = [&](int p) {
-    const int sl = slot(p);
-    for (int e = tid; e < NX * NY; e += NT) {
-      const int nxl = e % NX, nyl = e / NX;
-      const int gi = x0 - 1 + nxl, gj = y0 - 1 + nyl;
-      R v[6];
-      const bool in_range = gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy && p >= -1 && p <= g.sz;
-      const bool out_x = gi < 0 || gi >= g.sx, out_y = gj < 0 || gj >= g.sy, out_z = p < 0 || p >= g.sz;
-      const bool frozen = (out_x && !per_x) || (out_y && !per_y) || (out_z && !per_z);
-      const int ox = nxl + 1, oy = nyl + 1;  // OLD coordinates
-      if (!in_range) {
+    if (tid >= NCELL) return;
+    R* dst = nw + new_slot(p) * 6 * S::NEWPL + toff_new;
+    const R* o1 = old + old_slot(p) * 6 * S::OLDBOX + toff_old;
+    R v[6];
+    const bool in_range = xy_in && p >= -1 && p <= g.sz;
+    const bool frozen = out_xy_open || ((p < 0 || p >= g.sz) && !per_z);
+    if (!in_range) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v[c] = R(0);
-      } else if (frozen) {
+      for (int c = 0; c < 6; ++c) v[c] = R(0);
+    } else if (frozen) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v[c] = old[((sl * 6 + c) * HY + oy) * HX + ox];
-      } else {
-        SmemOld<R> a;
-        a.old = old;
-        a.b0 = P.b0;
-        a.gs = g.idx(gi, gj, p);
-        a.dj = g.px;
-        a.dk = g.plane;
-        a.x = ox;
-        a.y = oy;
-        a.s[0] = slot(p - 1);
-        a.s[1] = sl;
-        a.s[2] = slot(p + 1);
-        R d[6];
-        push_cell<R, C, B0>(a, P.cc, d);
+      for (int c = 0; c < 6; ++c) v[c] = o1[c * S::OLDBOX];
+    } else {
+      SmemOld<R> a;
+      a.b[0] = old + old_slot(p - 1) * 6 * S::OLDBOX + toff_old;
+      a.b[1] = o1;
+      a.b[2] = old + old_slot(p + 1) * 6 * S::OLDBOX + toff_old;
+      a.b0 = P.b0;
+      a.gs = gbase + (long long)p * g.plane;
+      a.dj = g.px;
+      a.dk = g.plane;
+      R d[6];
+      push_cell<R, C, B0, SmemOld<R>, FD>(a, P.cc, d);
+      const R* e1 = STAGE1 ? o1 : en + en_slot(p) * 6 * S::ENBOX + toff_en;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-          const R f = old[((sl * 6 + c) * HY + oy) * HX + ox];
-          const R fn = STAGE1 ? f : P.en[c][a.gs];
-          v[c] = combine<R, C>(P.c1, P.c2, P.c3, fn, f, d[c], P.incr != 0);
-        }
-        if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, gi + P.p.y0, p + P.p.z0, v);
+      for (int c = 0; c < 6; ++c) {
+        const R f = o1[c * S::OLDBOX];
+        const R fn = STAGE1 ? f : e1[c * S::ENBOX];
+        v[c] = combine<R, C>(P.c1, P.c2, P.c3, fn, f, d[c], P.incr != 0);
       }
-#pragma unroll
-      for (int c = 0; c < 6; ++c) nw[((sl * 6 + c) * NY + nyl) * NX + nxl] = v[c];
+      if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, gi + P.p.y0, p + P.p.z0, v);
     }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) dst[c * S::NEWPL] = v[c];
   };
 
+  const int lx = tid % TX, ly = tid / TX;  // output cell of this thread (tid < TX*TY)
+  const int ci = x0 + lx, cj = y0 + ly;
+  const bool c_in = tid < TX * TY && ci < g.sx && cj < g.sy;
+  // periodic images of this column in x and y (two per axis when s < 4)
+  int xs[3] = {ci, ci, ci}, ys[3] = {cj, cj, cj};
+  int nxs = 1, nys = 1;
+  if (per_x && ci < NG) xs[nxs++] = ci + g.sx;
+  if (per_x && ci >= g.sx - NG) xs[nxs++] = ci - g.sx;
+  if (per_y && cj < NG) ys[nys++] = cj + g.sy;
+  if (per_y && cj >= g.sy - NG) ys[nys++] = cj - g.sy;
+  const bool xy_images = nxs > 1 || nys > 1;
+  const int toff_c = (ly + 1) * NX + (lx + 1);
+
   auto clean_store = [&](int k) {
-    const int lx = tid % TX, ly = tid / TX;
-    const int gi = x0 + lx, gj = y0 + ly;
-    if (gi >= g.sx || gj >= g.sy) return;
+    if (!c_in) return;
     SmemNew<R> a;
-    a.nw = nw;
-    a.x = lx + 1;
-    a.y = ly + 1;
-    a.s[0] = slot(k - 1);
-    a.s[1] = slot(k);
-    a.s[2] = slot(k + 1);
+    a.b[0] = nw + new_slot(k - 1) * 6 * S::NEWPL + toff_c;
+    a.b[1] = nw + new_slot(k) * 6 * S::NEWPL + toff_c;
+    a.b[2] = nw + new_slot(k + 1) * 6 * S::NEWPL + toff_c;
     R e[3];
-    clean_cell<R, C>(a, e);
-    R v[6] = {e[0], e[1], e[2], a(BX, 0, 0, 0), a(BY, 0, 0, 0), a(BZ, 0, 0, 0)};
-    // the cell and its periodic images in the ghost shell (two per axis when s < 4)
-    int xs[3] = {gi, gi, gi}, ys[3] = {gj, gj, gj}, zs[3] = {k, k, k};
-    int nxs = 1, nys = 1, nzs = 1;
-    if (per_x && gi < NG) xs[nxs++] = gi + g.sx;
-    if (per_x && gi >= g.sx - NG) xs[nxs++] = gi - g.sx;
-    if (per_y && gj < NG) ys[nys++] = gj + g.sy;
-    if (per_y && gj >= g.sy - NG) ys[nys++] = gj - g.sy;
+    clean_cell<R, C, SmemNew<R>, FD>(a, e, P.ct);
+    const R v[6] = {e[0], e[1], e[2], a(BX, 0, 0, 0), a(BY, 0, 0, 0), a(BZ, 0, 0, 0)};
+    const bool z_image = per_z && (k < NG || k >= g.sz - NG);
+    if (!xy_images && !z_image) {
+      const long long o = g.idx(ci, cj, k);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) P.out[c][o] = v[c];
+      return;
+    }
+    int zs[3] = {k, k, k}, nzs = 1;
     if (per_z && k < NG) zs[nzs++] = k + g.sz;
     if (per_z && k >= g.sz - NG) zs[nzs++] = k - g.sz;
     for (int a2 = 0; a2 < nzs; ++a2)
@@ -180,22 +308,33 @@ __global__ void __launch_bounds__(NT) k_fused(const Params<R> P) {
         }
   };
 
-  load_old(kb - 2);
-  load_old(kb - 1);
-  load_old(kb);
-  __syncthreads();
-  compute_new(kb - 1);
-  __syncthreads();
-  load_old(kb + 1);
-  __syncthreads();
-  compute_new(kb);
-  __syncthreads();  // compute_new(kb) reads OLD(kb-1), whose slot load_old(kb+2) reuses
-  for (int k = kb; k < ke; ++k) {
-    load_old(k + 2);
+  // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
+  bool failed = !wait_planes(kb - 2, kb - 1) || !wait_planes(kb - 1, kb - 1) || !wait_planes(kb, kb - 1);
+  if (!__syncthreads_or(failed)) {
+    compute_new(kb - 1);
+    failed = !wait_planes(kb + 1, kb);
+    if (!__syncthreads_or(failed)) {
+      compute_new(kb);
+      __syncthreads();
+      // ---- march: one barrier per plane ------------------------------------
+      for (int k = kb; k < ke; ++k) {
+        refill(k);
+        failed = !wait_planes(k + 2, k + 1);
+        if (!failed) compute_new(k + 1);
+        if (__syncthreads_or(failed)) break;
+        clean_store(k);
+      }
+    }
+  }
+  if (failed) {
+    if (tid == 0) {
+      atomicExch(P.err, 1);
+      // drain the copies that may still be in flight: the last use of each slot
+      for (int p = max(kb - 2, old_next - DO); p < old_next; ++p) mbar_wait(bar_old + 8 * old_slot(p), old_par(p));
+      if (!STAGE1)
+        for (int p = max(kb - 1, en_next - DE); p < en_next; ++p) mbar_wait(bar_en + 8 * en_slot(p), en_par(p));
+    }
     __syncthreads();
-    compute_new(k + 1);
-    __syncthreads();
-    clean_store(k);
   }
 }
 
@@ -208,10 +347,13 @@ __global__ void __launch_bounds__(NT) k_fused(const Params<R> P) {
 #endif
 
 template <typename R, bool C>
-void FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
-                     const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0, const EB<R>& out,
-                     cudaStream_t st) {
+int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
+                    const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
+                    int* err, cudaStream_t st) {
   using namespace FFE_FUSED_NS;
+  Maps M;
+  memcpy(M.in, maps_in, sizeof(M.in));
+  memcpy(M.en, maps_en, sizeof(M.en));
   Params<R> P;
   P.g = g;
   P.p = p;
@@ -220,28 +362,32 @@ void FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R 
   P.c1 = c1;
   P.c2 = c2;
   P.c3 = c3;
+  P.ct = ct;
   P.incr = incr ? 1 : 0;
-  for (int c = 0; c < 6; ++c) {
-    P.in[c] = in.c[c];
-    P.en[c] = en.c[c];
-    P.out[c] = out.c[c];
-  }
+  for (int c = 0; c < 6; ++c) P.out[c] = out.c[c];
   for (int c = 0; c < 3; ++c) P.b0[c] = b0.c[c];
+  P.err = err;
   const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
-  // enough blocks for ~16 per SM on 152 SMs, at least 4 planes per block
-  long long want = 152LL * 16;
-  int kz = (int)std::max(4LL, std::min<long long>(64, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
+  // enough blocks for ~16 per SM on 152 SMs, at least 8 planes per block
+  const long long want = 152LL * 16;
+  int kz = (int)std::max(8LL, std::min<long long>(64, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
   kz = std::min(kz, g.sz);
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
-  const size_t smem = sizeof(R) * (3 * 6 * HY * HX + 3 * 6 * NY * NX);
+  const size_t smem = Sizes<R>::BYTES;
   const bool abs = p.bnd[0] == 2;
   const bool s1 = stage == 1;
-#define FFE_GO(B0V, ABSV, S1V)                                                                    \
-  do {                                                                                            \
-    auto kf = k_fused<R, C, B0V, ABSV, S1V>;                                                      \
-    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);             \
-    kf<<<grid, NT, smem, st>>>(P);                                                                \
+#define FFE_GO(B0V, ABSV, S1V)                                                                   \
+  do {                                                                                           \
+    auto kf = k_fused<R, C, B0V, ABSV, S1V>;                                                     \
+    static bool attr_set = false;                                                                \
+    if (!attr_set) {                                                                             \
+      if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
+          cudaSuccess)                                                                           \
+        return -3;                                                                               \
+      attr_set = true;                                                                           \
+    }                                                                                            \
+    kf<<<grid, NT, smem, st>>>(M, P);                                                            \
   } while (0)
   if (has_b0) {
     if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
@@ -251,6 +397,7 @@ void FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R 
     else { if (s1) FFE_GO(false, false, true); else FFE_GO(false, false, false); }
   }
 #undef FFE_GO
+  return 0;
 }
 
 #ifndef FFE_FUSED_EXACT
@@ -258,11 +405,39 @@ void fused_tile_shape(int* tx, int* ty) {
   *tx = fused_fast::TX;
   *ty = fused_fast::TY;
 }
+
+// Tensor maps of one array for the fused kernels: the OLD box (tile + 2 halo)
+// and the EN box (tile + 1 halo rows).  Coordinates: (i + 2, j + 2, k + 2).
+int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return -1;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  using namespace fused_fast;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.px, (cuuint64_t)g.py, (cuuint64_t)(g.sz + 2 * NG)};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.px * es, (cuuint64_t)g.plane * es};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const cuuint32_t box_old[3] = {(cuuint32_t)OW, (cuuint32_t)OH, 1};
+  const cuuint32_t box_en[3] = {(cuuint32_t)OW, (cuuint32_t)EH, 1};
+  CUresult r = encode((CUtensorMap*)map_old, dt, 3, base, dims, strides, box_old, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return -2;
+  r = encode((CUtensorMap*)map_en, dt, 3, base, dims, strides, box_en, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -2;
+}
 #endif
 
-#define FFE_INST_F(R, C)                                                                                          \
-  template void FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,         \
-                                      const CEB<R>&, const CEB<R>&, const CEB<R>&, bool, const EB<R>&, cudaStream_t);
+#define FFE_INST_F(R, C)                                                                                        \
+  template int FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,        \
+                                     const void*, const void*, const CEB<R>&, bool, const EB<R>&, R, int*,      \
+                                     cudaStream_t);
 FFE_INST_F(float, false)
 FFE_INST_F(float, true)
 FFE_INST_F(double, false)

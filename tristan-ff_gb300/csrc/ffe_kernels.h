@@ -16,7 +16,7 @@ template <typename R, bool C>
 void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2, R c3, bool incr, const EB<R>& f,
                    const CEB<R>& fn, const CEB<R>& df, cudaStream_t st);
 template <typename R, bool C>
-void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, cudaStream_t st);
+void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStream_t st);
 template <typename R>
 void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st);
 template <typename R>
@@ -44,11 +44,20 @@ void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
 // One launch advances one SSP-RK3 stage AND applies the E-parallel cleaning
 // of that stage: reads the stage input E,B (set `in`) and, for stages 2-3,
 // the step-start fields (set `en`); writes cleaned E and updated B to `out`.
-struct FusedArgs;
+// maps_in / maps_en: 6 CUtensorMaps each (ex..bz of the input set and of the
+// step-start set) made by make_stage_maps; err: device word set on a timeout.
+// Returns 0, or -3 if the kernel attribute could not be set.
+// ct: TINY added to the cleaning denominators (FFE_FLAG_CLEAN_TINY) or 0.
 template <typename R, bool C>
-void launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
-                        int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0, const EB<R>& out,
-                        cudaStream_t st);
+int launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
+                       int stage, const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0,
+                       const EB<R>& out, R ct, int* err, cudaStream_t st);
+template <typename R, bool C>
+int launch_fused_stage_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
+                             int stage, const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0,
+                             const EB<R>& out, R ct, int* err, cudaStream_t st);
+// The two TMA tensor maps (OLD box, EN box) of one field array at `base`.
+int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es);
 // Tile shape the fused kernel uses (for reporting).
 void fused_tile_shape(int* tx, int* ty);
 

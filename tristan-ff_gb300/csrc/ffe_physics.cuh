@@ -27,18 +27,26 @@ __device__ __forceinline__ R rho_at(const A& a, int di, int dj, int dk) {
          (a(EZ, di, dj, dk) - a(EZ, di, dj, dk - 1));
 }
 
+// Quotient x / y: correctly rounded, or (FD, float only) the two-instruction
+// reciprocal-multiply of __fdividef (<= 2 ulp) used by the fast fused path.
+template <typename R, bool FD>
+__device__ __forceinline__ R qdiv(R x, R y) {
+  if constexpr (FD && sizeof(R) == 4) return __fdividef(x, y);
+  else return x / y;
+}
+
 // J = CC rho (E x B) / (B^2 + TINY) with the denominator in R, or in double (FP32C).
-template <typename R, bool C>
+template <typename R, bool C, bool FD = false>
 __device__ __forceinline__ R jdiv(R cc, R bmag, R bx, R by, R bz, R num) {
   if (C) {
     const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
     return (R)((double)cc / (bd + (double)tiny<float>()) * (double)num);
   }
-  return cc / (bmag + tiny<R>()) * num;
+  return qdiv<R, FD>(cc, bmag + tiny<R>()) * num;
 }
 
 // rk3Push (field_solver.F90:81-162): writes dE (with -J) and dB of one cell.
-template <typename R, bool C, bool B0, class A>
+template <typename R, bool C, bool B0, class A, bool FD = false>
 __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
   const R ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -72,11 +80,11 @@ __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   emag = (intex * intex + intey * intey) + intez * intez;
   if (emag > bmag) {
-    const R corr = sqrt(bmag / emag);
+    const R corr = sqrt(qdiv<R, FD>(bmag, emag));
     intey = intey * corr;
     intez = intez * corr;
   }
-  const R jx = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intey * intbz - intby * intez));
+  const R jx = jdiv<R, C, FD>(cc, bmag, intbx, intby, intbz, intrho * (intey * intbz - intby * intez));
   // Y current (:114-134)
   intrho = R(0.5) * (a.rho(0, 1, 0) + r0);
   intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0));
@@ -89,11 +97,11 @@ __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   emag = (intex * intex + intey * intey) + intez * intez;
   if (emag > bmag) {
-    const R corr = sqrt(bmag / emag);
+    const R corr = sqrt(qdiv<R, FD>(bmag, emag));
     intex = intex * corr;
     intez = intez * corr;
   }
-  const R jy = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intez * intbx - intex * intbz));
+  const R jy = jdiv<R, C, FD>(cc, bmag, intbx, intby, intbz, intrho * (intez * intbx - intex * intbz));
   // Z current (:137-157)
   intrho = R(0.5) * (r0 + a.rho(0, 0, 1));
   intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1));
@@ -106,11 +114,11 @@ __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   emag = (intex * intex + intey * intey) + intez * intez;
   if (emag > bmag) {
-    const R corr = sqrt(bmag / emag);
+    const R corr = sqrt(qdiv<R, FD>(bmag, emag));
     intex = intex * corr;
     intey = intey * corr;
   }
-  const R jz = jdiv<R, C>(cc, bmag, intbx, intby, intbz, intrho * (intex * intby - intbx * intey));
+  const R jz = jdiv<R, C, FD>(cc, bmag, intbx, intby, intbz, intrho * (intex * intby - intbx * intey));
   d[0] = d[0] - jx;
   d[1] = d[1] - jy;
   d[2] = d[2] - jz;
@@ -148,17 +156,18 @@ __device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int j
 }
 
 // cleanEpar (field_solver.F90:288-328): E - (E.B) B / B^2 at the three E points.
-template <typename R, bool C>
-__device__ __forceinline__ R clean_div(R epar, R bi, R bmag, R bx, R by, R bz) {
+template <typename R, bool C, bool FD = false>
+__device__ __forceinline__ R clean_div(R epar, R bi, R bmag, R bx, R by, R bz, R ct) {
+  // ct = 0 (the reference) or TINY (FFE_FLAG_CLEAN_TINY); bmag + 0 == bmag exactly
   if (C) {
     const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
-    return (R)((double)(epar * bi) / bd);
+    return (R)((double)(epar * bi) / (bd + (double)ct));
   }
-  return epar * bi / bmag;
+  return qdiv<R, FD>(epar * bi, bmag + ct);
 }
 
-template <typename R, bool C, class A>
-__device__ __forceinline__ void clean_cell(const A& a, R e[3]) {
+template <typename R, bool C, class A, bool FD = false>
+__device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
   const R ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
   R intex, intey, intez, intbx, intby, intbz, bmag, epar;
@@ -171,7 +180,7 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3]) {
   intbz = R(0.5) * (bz0 + a(BZ, 0, -1, 0));
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   epar = (intex * intbx + intey * intby) + intez * intbz;
-  e[0] = ex0 - clean_div<R, C>(epar, intbx, bmag, intbx, intby, intbz);
+  e[0] = ex0 - clean_div<R, C, FD>(epar, intbx, bmag, intbx, intby, intbz, ct);
 
   intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0));
   intey = ey0;
@@ -182,7 +191,7 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3]) {
   intbz = R(0.5) * (bz0 + a(BZ, -1, 0, 0));
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   epar = (intex * intbx + intey * intby) + intez * intbz;
-  e[1] = ey0 - clean_div<R, C>(epar, intby, bmag, intbx, intby, intbz);
+  e[1] = ey0 - clean_div<R, C, FD>(epar, intby, bmag, intbx, intby, intbz, ct);
 
   intex = R(0.25) * (((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1));
   intey = R(0.25) * (((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1));
@@ -193,7 +202,7 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3]) {
                         a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1));
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   epar = (intex * intbx + intey * intby) + intez * intbz;
-  e[2] = ez0 - clean_div<R, C>(epar, intbz, bmag, intbx, intby, intbz);
+  e[2] = ez0 - clean_div<R, C, FD>(epar, intbz, bmag, intbx, intby, intbz, ct);
 }
 
 }  // namespace ffe

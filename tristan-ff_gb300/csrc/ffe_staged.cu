@@ -79,7 +79,7 @@ __global__ void k_update(Geom g, Phys p, Absorb<R> ab, R c1, R c2, R c3, int inc
 
 // ---- cleanEpar into dE, then dE -> E over the interior (:284-334) ---------
 template <typename R, bool C>
-__global__ void k_clean(Geom g, CEB<R> eb, R* __restrict__ dex, R* __restrict__ dey, R* __restrict__ dez) {
+__global__ void k_clean(Geom g, CEB<R> eb, R* __restrict__ dex, R* __restrict__ dey, R* __restrict__ dez, R ct) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -90,7 +90,7 @@ __global__ void k_clean(Geom g, CEB<R> eb, R* __restrict__ dex, R* __restrict__ 
   a.dj = g.px;
   a.dk = g.plane;
   R e[3];
-  clean_cell<R, C>(a, e);
+  clean_cell<R, C>(a, e, ct);
   dex[a.s] = e[0];
   dey[a.s] = e[1];
   dez[a.s] = e[2];
@@ -483,11 +483,11 @@ void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2
 }
 
 template <typename R, bool C>
-void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, cudaStream_t st) {
+void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStream_t st) {
   const dim3 gr = grid_for(g.sx, g.sy, g.sz, B2);
   CEB<R> c;
   for (int i = 0; i < 6; ++i) c.c[i] = eb.c[i];
-  k_clean<R, C><<<gr, B2, 0, st>>>(g, c, d.c[0], d.c[1], d.c[2]);
+  k_clean<R, C><<<gr, B2, 0, st>>>(g, c, d.c[0], d.c[1], d.c[2], ct);
   k_copy_e<R><<<gr, B2, 0, st>>>(g, d.c[0], d.c[1], d.c[2], eb.c[0], eb.c[1], eb.c[2]);
 }
 
@@ -610,7 +610,7 @@ template int launch_waves<double>(const Geom&, const Phys&, const double[3], int
                                   cudaStream_t);                                                              \
   template void launch_update<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, bool, const EB<R>&,   \
                                     const CEB<R>&, const CEB<R>&, cudaStream_t);                              \
-  template void launch_clean<R, C>(const Geom&, const EB<R>&, const EB<R>&, cudaStream_t);
+  template void launch_clean<R, C>(const Geom&, const EB<R>&, const EB<R>&, R, cudaStream_t);
 
 FFE_INST_R(float)
 FFE_INST_R(double)
