@@ -186,6 +186,23 @@ int ffe_user_bc(ffe_t h, int32_t step);
    K[3] (radians per cell), phi, a, u[3] (unit polarisation), n[3]; nmodes <= 64. */
 int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* modes);
 
+/* cleanEpar on arrays the caller owns, with no device allocation by the
+   library.  No counterpart in the reference: it is for callers that manage
+   all of their device memory themselves (arrays reserved once to fill HBM, or
+   a run loop where an allocation call, which may synchronise the device or
+   fail on fragmented memory, is not acceptable).  ex..bz are device pointers
+   to arrays in the reference's layout ((sx+4)(sy+4)(sz+4), x fastest, cell
+   -2 first); E is cleaned in place.  The out-of-place scratch is a fixed
+   24 MiB device array inside the library, so 3*sx*sy*sz values must fit
+   (2,097,152 interior cells in FP32, 1,048,576 in FP64); larger sizes
+   return FFE_EINVAL.  The first call on a device looks up the scratch's
+   device address (make it before any stream capture).  All calls share the
+   scratch: calls that overlap on the GPU race.  Asynchronous on `stream`
+   (a cudaStream_t, NULL = the default stream); errors read back with
+   ffe_last_error(NULL, ...).                                               */
+int ffe_clean_epar_noalloc(int32_t sx, int32_t sy, int32_t sz, int32_t precision, void* ex, void* ey, void* ez,
+                           const void* bx, const void* by, const void* bz, void* stream);
+
 /* --- whole steps -------------------------------------------------------- */
 /* exchangeFields(exchangeB0=.true.) then userFieldBoundaryConditions(0). */
 int ffe_mainloop_prologue(ffe_t h);

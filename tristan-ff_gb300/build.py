@@ -29,6 +29,7 @@ UNITS = [
     ("ffe_staged.cu", "ffe_staged.o", ["-fmad=false"]),
     ("ffe_fused.cu", "ffe_fused_fast.o", []),
     ("ffe_fused.cu", "ffe_fused_exact.o", ["-fmad=false", "-DFFE_FUSED_EXACT"]),
+    ("ffe_noalloc.cu", "ffe_noalloc.o", ["-fmad=false"]),
 ]
 
 

@@ -44,11 +44,9 @@ int set_thread_err(int st, const char* fmt, ...) {
   return st;
 }
 
-struct Engine {
-  virtual ~Engine() {}
-};
-
 }  // namespace
+
+int ffe::set_thread_error(int status, const char* msg) { return set_thread_err(status, "%s", msg); }
 
 struct ffe_solver {
   ffe_grid_desc d;

@@ -61,4 +61,7 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
 // Tile shape the fused kernel uses (for reporting).
 void fused_tile_shape(int* tx, int* ty);
 
+// Record a failure without a handle (read back by ffe_last_error(NULL, ...)).
+int set_thread_error(int status, const char* msg);
+
 }  // namespace ffe

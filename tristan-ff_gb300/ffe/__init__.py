@@ -59,6 +59,7 @@ ABI_SYMBOLS = (
     "ffe_clean_epar", "ffe_exchange_fields", "ffe_user_initialize", "ffe_user_bc",
     "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
     "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
+    "ffe_clean_epar_noalloc",
 )
 
 
@@ -144,6 +145,8 @@ def load_library(path=None):
         "ffe_synchronize": [H],
         "ffe_synchronize_timeout": [H, i32],
         "ffe_init_waves": [H, ctypes.POINTER(ctypes.c_double), i32, ctypes.POINTER(ctypes.c_double)],
+        "ffe_clean_epar_noalloc": [i32, i32, i32, i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
