@@ -47,10 +47,91 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c", "fp32cd", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of timing: run FP64, FP32 and FP32C for N steps and report their errors")
+    ap.add_argument("--oracle-steps", type=int, default=0,
+                    help="with --accuracy-steps: also check the FP64 GPU path against the CPU oracle "
+                         "after this many steps")
     return ap.parse_args()
+
+
+def accuracy(args):
+    """Relative L2 and L-infinity error of E and B of the FP32 and FP32C fused
+    paths against the FP64 fused path after N steps of the benchmark workload.
+    The FP64 GPU path stands in for the CPU oracle at this size; it is first
+    checked against the oracle (FP64, OpenMP) over `--oracle-steps` steps."""
+    import numpy as np
+    import torch
+    import ffe
+    import build as ffe_build
+    torch.cuda.set_device(0)
+    ffe_build.build()
+    S = args.size
+    size = (S, S, S)
+    bg, modes = workload(S)
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+
+    def run(prec, steps):
+        g = ffe.Solver(ffe.make_desc(size, precision=prec))
+        g.init_waves(bg, modes)
+        g.mainloop_prologue()
+        init = None
+        if prec == ffe.FP64 and args.oracle_steps:
+            init = {n: g.download(n) for n in names}
+        t0 = time.perf_counter()
+        g.mainloop(steps, 0)
+        g.synchronize()
+        dt = time.perf_counter() - t0
+        out = {n: ffe.interior(g.download(n)) for n in names}
+        g.close()
+        return out, dt, init
+
+    def errors(a, b):
+        res = {}
+        for grp, comps in (("E", names[:3]), ("B", names[3:])):
+            num2 = den2 = linf = dmax = 0.0
+            for n in comps:
+                x = a[n].astype(np.float64)
+                y = b[n]
+                d = x - y
+                num2 += float(np.vdot(d, d).real)
+                den2 += float(np.vdot(y, y).real)
+                linf = max(linf, float(np.max(np.abs(d))))
+                dmax = max(dmax, float(np.max(np.abs(y))))
+            res[grp] = {"rel_l2": (num2 / den2) ** 0.5 if den2 else None, "rel_linf": linf / dmax if dmax else None}
+        return res
+
+    N = args.accuracy_steps
+    ref, t64, init = run(ffe.FP64, N)
+    line = {"metric": "relative error vs the FP64 path after %d steps" % N, "grid": [S] * 3,
+            "workload": "random Alfven+fast modes, periodic", "fp64_seconds": t64}
+    for name, prec in (("fp32", ffe.FP32), ("fp32c", ffe.FP32C), ("fp32cd", ffe.FP32CD)):
+        out, dt, _ = run(prec, N)
+        line[name] = errors(out, ref)
+        line[name]["seconds"] = dt
+        del out
+    if args.oracle_steps:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        k = args.oracle_steps
+        g = ffe.Solver(ffe.make_desc(size, precision=ffe.FP64))
+        g.set_fields(init)
+        g.mainloop(k, 0)
+        gpu = {n: ffe.interior(g.download(n)) for n in names}
+        g.close()
+        o = O.Oracle(ffe.make_desc(size, precision=ffe.FP64), threads=os.cpu_count() or 1, loop_order=1)
+        o.set_fields(init)
+        t0 = time.perf_counter()
+        o.mainloop(k, 0)
+        cpu = {n: ffe.interior(o.download(n)) for n in names}
+        line["fp64_gpu_vs_cpu_oracle"] = errors(gpu, cpu)
+        line["fp64_gpu_vs_cpu_oracle"]["steps"] = k
+        line["fp64_gpu_vs_cpu_oracle"]["oracle_seconds"] = time.perf_counter() - t0
+    print(json.dumps(line), flush=True)
 
 
 def dist_env():
@@ -153,7 +234,7 @@ def cpu_baseline(args, edge=None, steps=None, threads=None):
     steps = steps or 100
     size = (edge, edge, edge)
     bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
-    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    prec = ffe.PRECISIONS[args.precision]
     o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
     o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
     o.mainloop_prologue()
@@ -182,7 +263,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     size = (edge, edge, edge)
     bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
-    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    prec = ffe.PRECISIONS[args.precision]
     o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
     o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
     o.mainloop_prologue()
@@ -211,6 +292,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.accuracy_steps:
+        accuracy(args)
+        return
     import numpy as np
     import torch
     import ffe
@@ -228,7 +312,7 @@ def main():
 
     S = args.size
     size = (S, S, S)
-    prec = {"fp32": ffe.FP32, "fp32c": ffe.FP32C, "fp64": ffe.FP64}[args.precision]
+    prec = ffe.PRECISIONS[args.precision]
     stream = torch.cuda.Stream()
     desc = ffe.make_desc(size, precision=prec, stream=stream.cuda_stream)
     g = ffe.Solver(desc)

@@ -72,8 +72,10 @@ typedef enum {
 typedef enum {
   FFE_FP64 = 0,  /* every real is double: what a -fdefault-real-8 build computes */
   FFE_FP32 = 1,  /* every real is float: the arithmetic of the shipped build      */
-  FFE_FP32C = 2  /* float storage; increment-form (compensated) RK combination;
-                    B^2 denominators of the current and the cleaning in double  */
+  FFE_FP32C = 2, /* float storage; increment-form (compensated) RK combination
+                    En + (c2 (E - En) + c3 dE): no drift from 1/3 + 2/3 != 1 in float */
+  FFE_FP32CD = 3 /* FFE_FP32C with the B^2 denominators of the current and of
+                    the cleaning in double (slow where FP64 is slow, as on GB300) */
 } ffe_precision;
 
 typedef enum {

@@ -43,6 +43,7 @@ CASES = [
     ("random_fp32_absorb", (11, 9, 8), ffe.FP32, (2, 2, 2), 0, (), 2, "random"),
     ("random_fp64_mixed", (10, 7, 6), ffe.FP64, (1, 1, 0), 0, (), 2, "random"),
     ("random_fp32c_periodic", (9, 8, 7), ffe.FP32C, (1, 1, 1), 0, (), 2, "random"),
+    ("random_fp32cd_periodic", (9, 8, 7), ffe.FP32CD, (1, 1, 1), 0, (), 2, "random"),
     ("psr_fp64_open", (20, 20, 20), ffe.FP64, (0, 0, 0), 1, (4.0, 30.0, 120.0, 1.0), 3, "setup"),
     ("uniform_fp32_tube", (12, 12, 10), ffe.FP32, (1, 1, 0), 2, (8.0, 0.4, 5.0, 0.3), 3, "setup"),
     ("loop_fp64", (12, 12, 10), ffe.FP64, (1, 1, 0), 3, (3.0, 1.0, 1.0, 0.5, 5.0, 0.3), 3, "setup"),
@@ -69,7 +70,7 @@ def main():
         o.mainloop_prologue()
         o.mainloop(steps, 0)
         out = o.fields()
-        if setup == 0 and prec != ffe.FP32C:
+        if setup == 0 and prec in (ffe.FP32, ffe.FP64):
             n = NumpySolver(*size, dt, boundary=bnd, absorb_buff=3)
             for k, v in f.items():
                 n.f[k][...] = v

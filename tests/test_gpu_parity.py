@@ -18,7 +18,7 @@ from test_oracle_cpu import random_fields
 pytestmark = pytest.mark.gpu
 
 F6 = ("ex", "ey", "ez", "bx", "by", "bz")
-PRECS = [ffe.FP64, ffe.FP32, ffe.FP32C]
+PRECS = [ffe.FP64, ffe.FP32, ffe.FP32C, ffe.FP32CD]
 BNDS = [(1, 1, 1), (0, 0, 0), (2, 2, 2), (1, 1, 0)]
 
 
@@ -86,14 +86,6 @@ def test_staged_procedures_bit_exact(oracle_mod, prec, bnd):
 @pytest.mark.parametrize("path", [ffe.PATH_STAGED, ffe.PATH_FUSED_EXACT])
 def test_steps_bit_exact(oracle_mod, prec, bnd, path):
     g, o = pair(oracle_mod, (37, 19, 11), prec, bnd, path)
-    mixed = 1 in bnd and any(b != 1 for b in bnd)
-    if path == ffe.PATH_FUSED_EXACT and mixed:
-        # ghosts outside both a periodic and an open face are not periodic images:
-        # the fused kernels refuse such grids (they run staged under PATH_AUTO)
-        with pytest.raises(ffe.FFEError) as e:
-            g.mainloop(1, 0)
-        assert e.value.status == -7
-        return
     for s in (g, o):
         s.mainloop_prologue()
         s.mainloop(3, 0)
@@ -102,7 +94,7 @@ def test_steps_bit_exact(oracle_mod, prec, bnd, path):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("bnd", [(1, 1, 1), (2, 2, 2), (0, 0, 0)])
+@pytest.mark.parametrize("bnd", [(1, 1, 1), (2, 2, 2), (0, 0, 0), (1, 1, 0), (0, 1, 1)])
 def test_fused_fast_matches_oracle(oracle_mod, prec, bnd):
     size = (40, 24, 20)
     # without the clamp the absorbing corners amplify every rounding difference
@@ -126,11 +118,12 @@ def test_fused_fast_matches_oracle(oracle_mod, prec, bnd):
 def test_fused_tiles_cover_ragged_sizes(oracle_mod):
     """Sizes that are not multiples of the 32x8 tile or of the z chunk."""
     for size in [(33, 9, 5), (70, 17, 13), (2, 2, 2), (5, 31, 3)]:
-        g, o = pair(oracle_mod, size, ffe.FP64, (1, 1, 1), ffe.PATH_FUSED_EXACT, b0=False)
-        for s in (g, o):
-            s.mainloop_prologue()
-            s.mainloop(2, 0)
-        assert_same(g, o)
+        for bnd in [(1, 1, 1), (1, 0, 1), (0, 1, 0)]:
+            g, o = pair(oracle_mod, size, ffe.FP64, bnd, ffe.PATH_FUSED_EXACT, b0=False)
+            for s in (g, o):
+                s.mainloop_prologue()
+                s.mainloop(2, 0)
+            assert_same(g, o)
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -200,9 +193,12 @@ def test_step_paths_and_launch_counts():
     g = ffe.Solver(ffe.make_desc((16, 16, 16), boundary=(2, 2, 2)))
     assert g.step_path() == ffe.PATH_FUSED
     g = ffe.Solver(ffe.make_desc((16, 16, 16), boundary=(1, 1, 0)))
-    assert g.step_path() == ffe.PATH_STAGED
+    assert g.step_path() == ffe.PATH_FUSED
     g = ffe.Solver(ffe.make_desc((16, 16, 16), setup=ffe.SETUP_PSR, params=(3.0, 10.0, 100.0),
                                  boundary=(0, 0, 0)))
+    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 12
+    g = ffe.Solver(ffe.make_desc((16, 16, 16), setup=ffe.SETUP_UNIFORM, params=(8.0, 0.4, 5.0, 0.3),
+                                 boundary=(1, 1, 0)))
     assert g.step_path() == ffe.PATH_STAGED
 
 
@@ -222,3 +218,37 @@ def test_large_grid_fp32_vs_fp64_gpu():
         eb = np.concatenate([res[prec][k].ravel() for k in F6])
         e64 = np.concatenate([res[ffe.FP64][k].ravel() for k in F6])
         assert rel_l2(eb, e64) < 1e-5, (prec, rel_l2(eb, e64))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("bnd,flags", [((0, 0, 0), 0),
+                                       ((2, 2, 2), ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY)])
+def test_psr_fused_equals_staged(prec, bnd, flags):
+    """The rotating-conductor BC on the fused path (fused stage + box fix-up)
+    gives the staged path's result bit for bit when both skip contraction."""
+    size = (40, 36, 34)
+    prm = (5.0, 30.0, 120.0, 1.0)
+    res = {}
+    for path in (ffe.PATH_STAGED, ffe.PATH_FUSED_EXACT):
+        g = ffe.Solver(ffe.make_desc(size, precision=prec, boundary=bnd, setup=ffe.SETUP_PSR, params=prm,
+                                     absorb_buff=5, flags=flags, path=path))
+        g.userInitialize()
+        g.mainloop_prologue()
+        g.mainloop(3, 7)
+        res[path] = g.fields()
+    for k in F6:
+        a, b = res[ffe.PATH_STAGED][k], res[ffe.PATH_FUSED_EXACT][k]
+        assert np.array_equal(a, b), (k, float(np.nanmax(np.abs(a.astype(float) - b))))
+
+
+def test_psr_fused_fast_matches_oracle(oracle_mod):
+    size = (40, 36, 34)
+    d = ffe.make_desc(size, precision=ffe.FP64, boundary=(0, 0, 0), setup=ffe.SETUP_PSR,
+                      params=(5.0, 30.0, 120.0, 1.0), path=ffe.PATH_FUSED)
+    g = ffe.Solver(d)
+    o = oracle_mod.Oracle(d)
+    for s in (g, o):
+        s.userInitialize()
+        s.mainloop_prologue()
+        s.mainloop(4, 0)
+    assert_same(g, o, exact=False, tol=1e-12)

@@ -208,29 +208,29 @@ template <typename R> UniformBC<R> uniform_consts(ffe_t h, int step) {
 // ---------------------------------------------------------------------------
 // precision-dispatched operations
 // ---------------------------------------------------------------------------
-template <typename R, bool C>
+template <typename R, int C>
 int op_rho(ffe_t h) {
   EB<R> e = eb_of<R>(h, h->cur);
   launch_rho<R>(h->g, e.c[0], e.c[1], e.c[2], (R*)h->rho, h->st);
   return check_launch(h, "computeRho");
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int op_push(ffe_t h) {
   launch_push<R, C>(h->g, R(h->d.cc), ceb_of<R>(h, h->cur), ceb_b0<R>(h), h->has_b0, (const R*)h->rho,
                     eb_of<R>(h, s_d(h)), h->st);
   return check_launch(h, "rk3Push");
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int op_update(ffe_t h, double c1, double c2, double c3) {
-  const bool incr = C && std::fabs(c1 + c2 - 1.0) < 1e-12;
+  const bool incr = C && std::fabs(c1 + c2 - 1.0) < 1e-6;
   launch_update<R, C>(h->g, h->p, absorb_consts<R>(h), R(c1), R(c2), R(c3), incr, eb_of<R>(h, h->cur),
                       ceb_of<R>(h, s_en(h)), ceb_of<R>(h, s_d(h)), h->st);
   return check_launch(h, "rk3Update");
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int op_clean(ffe_t h) {
   launch_clean<R, C>(h->g, eb_of<R>(h, h->cur), eb_of<R>(h, s_d(h)), clean_tiny<R>(h), h->st);
   return check_launch(h, "cleanEpar");
@@ -303,7 +303,7 @@ template <typename R> void stage_coeffs(int s, double c[3]) {
   else { c[0] = double(one / R(3.0)); c[1] = double(R(2.0) / R(3.0)); c[2] = double(R(2.0) / R(3.0)); }
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int step_staged(ffe_t h, int nsteps, int step0) {
   int rc;
   for (int n = 0; n < nsteps; ++n) {
@@ -324,15 +324,14 @@ int step_staged(ffe_t h, int nsteps, int step0) {
   return FFE_OK;
 }
 
-// The fused kernels compute halo cells on a periodic face from the arrays'
-// ghost values.  With mixed periodic/open axes, ghost cells that lie outside
-// both kinds of face keep frozen values that are not periodic images, so the
-// image of a cell next to an open face can differ: those grids run staged.
+// The fused kernels run every boundary combination (halo cells on a periodic
+// face next to an open face are computed at their periodic image).  The pulsar
+// BC runs on the fused path through a fix-up of its box when no axis is
+// periodic; the other user boundary conditions run staged.
 bool fused_possible(ffe_t h) {
   const int* b = h->d.boundary;
-  const bool all_per = b[0] == 1 && b[1] == 1 && b[2] == 1;
-  const bool none_per = b[0] != 1 && b[1] != 1 && b[2] != 1;
-  return h->d.setup == FFE_SETUP_NONE && (all_per || none_per) && h->maps_ok;
+  const bool any_per = b[0] == 1 || b[1] == 1 || b[2] == 1;
+  return h->maps_ok && (h->d.setup == FFE_SETUP_NONE || (h->d.setup == FFE_SETUP_PSR && !any_per));
 }
 
 template <typename R>
@@ -348,50 +347,81 @@ int sync_ghosts(ffe_t h) {
   return FFE_OK;
 }
 
-template <typename R, bool C>
-int step_fused(ffe_t h, int nsteps, bool exact) {
+// Elements of one of the two pulsar fix-up buffers: 6 components over the BC
+// box dilated by two cells.
+template <typename R> size_t psr_fix_elems(ffe_t h) {
+  const PsrBC<R> q = psr_consts<R>(h, 0);
+  if (q.bx <= 0 || q.by <= 0 || q.bz <= 0) return 0;
+  return (size_t)6 * (q.bx + 4) * (q.by + 4) * (q.bz + 4);
+}
+
+template <typename R, int C>
+int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
   int rc;
   if ((rc = sync_ghosts<R>(h))) return rc;
   const Absorb<R> ab = absorb_consts<R>(h);
   const CEB<R> b0 = ceb_b0<R>(h);
+  const bool psr = h->d.setup == FFE_SETUP_PSR;
+  R* s1 = (R*)h->box;
+  R* s2 = psr ? s1 + psr_fix_elems<R>(h) : nullptr;
   for (int n = 0; n < nsteps; ++n) {
     const int A = h->cur, B = (h->cur + 1) % 3, Cs = (h->cur + 2) % 3;
     const int ins[3] = {A, B, Cs}, outs[3] = {B, Cs, B};
+    PsrBC<R> q{};
+    if (psr) q = psr_consts<R>(h, step0 + n);
     for (int s = 0; s < 3; ++s) {
       double c[3];
       stage_coeffs<R>(s, c);
-      const bool incr = C && std::fabs(c[0] + c[1] - 1.0) < 1e-12;
+      // c1 + c2 = 1 exactly for SSP-RK3; in FP32 the rounded 1/3 + 2/3 misses by 3e-8
+      const bool incr = C && std::fabs(c[0] + c[1] - 1.0) < 1e-6;
       const void* mi = h->tm_old[ins[s]];
       const void* me = h->tm_en[A];
+      const R ct = clean_tiny<R>(h);
       int lr;
       if (exact)
         lr = launch_fused_stage_exact<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi,
-                                            me, b0, h->has_b0, eb_of<R>(h, outs[s]), clean_tiny<R>(h), h->derr,
-                                            h->st);
+                                            me, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0,
+                                            eb_of<R>(h, outs[s]), ct, h->derr, h->st);
       else
         lr = launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi, me,
-                                      b0, h->has_b0, eb_of<R>(h, outs[s]), clean_tiny<R>(h), h->derr, h->st);
+                                      ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
+                                      ct, h->derr, h->st);
       if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
       if ((rc = check_launch(h, "fused stage"))) return rc;
+      if (psr) {
+        if (exact)
+          launch_psr_fixup_exact<R, C>(h->g, h->p, ab, q, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1,
+                                       ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
+                                       ct, s1, s2, h->st);
+        else
+          launch_psr_fixup<R, C>(h->g, h->p, ab, q, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1,
+                                 ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]), ct,
+                                 s1, s2, h->st);
+        if ((rc = check_launch(h, "pulsar boundary fix-up"))) return rc;
+      }
     }
     h->cur = B;
   }
   return FFE_OK;
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int do_step(ffe_t h, int nsteps, int step0) {
   const int path = h->d.path;
   if (path == FFE_PATH_STAGED || (path == FFE_PATH_AUTO && !fused_possible(h))) return step_staged<R, C>(h, nsteps, step0);
   if (!fused_possible(h))
-    return fail(h, FFE_EUNSUPPORTED, "fused path needs setup NONE and all-periodic or all-non-periodic boundaries");
-  return step_fused<R, C>(h, nsteps, path == FFE_PATH_FUSED_EXACT);
+    return fail(h, FFE_EUNSUPPORTED,
+                "fused path: setup must be none, or psr with no periodic axis (other user BCs run staged)");
+  return step_fused<R, C>(h, nsteps, step0, path == FFE_PATH_FUSED_EXACT);
 }
 
-#define DISPATCH(h, FN, ...)                                                            \
-  ((h)->d.precision == FFE_FP64    ? FN<double, false>(__VA_ARGS__)                      \
-   : (h)->d.precision == FFE_FP32C ? FN<float, true>(__VA_ARGS__)                        \
-                                   : FN<float, false>(__VA_ARGS__))
+// precision -> (storage type, combination/denominator mode): 0 the reference's
+// arithmetic, 1 increment-form RK combination, 2 that plus double B^2 denominators
+#define DISPATCH(h, FN, ...)                                                             \
+  ((h)->d.precision == FFE_FP64     ? FN<double, 0>(__VA_ARGS__)                          \
+   : (h)->d.precision == FFE_FP32C  ? FN<float, 1>(__VA_ARGS__)                           \
+   : (h)->d.precision == FFE_FP32CD ? FN<float, 2>(__VA_ARGS__)                           \
+                                    : FN<float, 0>(__VA_ARGS__))
 #define DISPATCH_R(h, FN, ...) ((h)->d.precision == FFE_FP64 ? FN<double>(__VA_ARGS__) : FN<float>(__VA_ARGS__))
 
 int check_handle(ffe_t h) {
@@ -430,7 +460,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
                           d.sz, FFE_NGHOST);
   if (d.gsx < d.sx || d.gsy < d.sy || d.gsz < d.sz)
     return set_thread_err(FFE_EINVAL, "global mesh smaller than the meshblock");
-  if (d.precision < FFE_FP64 || d.precision > FFE_FP32C) return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
+  if (d.precision < FFE_FP64 || d.precision > FFE_FP32CD)
+    return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
   if (d.setup < FFE_SETUP_NONE || d.setup > FFE_SETUP_LOOP) return set_thread_err(FFE_EINVAL, "bad setup %d", d.setup);
   if (d.path < FFE_PATH_AUTO || d.path > FFE_PATH_FUSED_EXACT) return set_thread_err(FFE_EINVAL, "bad path %d", d.path);
   if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY)) || d.reserved)
@@ -478,13 +509,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   const size_t abytes = ((size_t)g.nelem * h->es + 255) / 256 * 256;
   size_t total = abytes * 22;
   if (d.setup == FFE_SETUP_PSR) {
-    PsrBC<float> q = dbl ? PsrBC<float>{} : psr_consts<float>(h, 0);
-    if (dbl) {
-      PsrBC<double> qd = psr_consts<double>(h, 0);
-      h->box_bytes = (size_t)qd.bx * qd.by * qd.bz * 6 * 8;
-    } else {
-      h->box_bytes = (size_t)q.bx * q.by * q.bz * 6 * 4;
-    }
+    // staged BC: 6 x box; fused fix-up: two buffers of 6 x (box + 2 cells)
+    h->box_bytes = 2 * (dbl ? psr_fix_elems<double>(h) * 8 : psr_fix_elems<float>(h) * 4);
     h->box_bytes = (h->box_bytes + 255) / 256 * 256;
     total += h->box_bytes;
   }
@@ -691,7 +717,8 @@ int ffe_step_launches(ffe_t h, int32_t* n) {
   int rc;
   if ((rc = ffe_step_path(h, &path))) return rc;
   if (path != FFE_PATH_STAGED) {
-    *n = 3;
+    // per stage: the fused kernel, plus the three box fix-up kernels of the pulsar BC
+    *n = h->d.setup == FFE_SETUP_PSR ? 12 : 3;
     return FFE_OK;
   }
   // per stage: rho, push, update, [bc], [fill], clean + copy, [fill]

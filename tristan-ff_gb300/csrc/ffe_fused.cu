@@ -41,6 +41,7 @@
 #include <cstring>
 #include "ffe_kernels.h"
 #include "ffe_physics.cuh"
+#include "ffe_psr.cuh"
 
 #ifdef FFE_FUSED_EXACT
 #define FFE_FUSED_NS fused_exact
@@ -88,8 +89,24 @@ struct Params {
   int incr;
   int kz;  // planes per block
   const R* b0[3];
+  const R* in_g[6];  // stage input and step-start sets in global memory, for the
+  const R* en_g[6];  // few halo cells computed at their periodic image (see below)
   R* out[6];
   int* err;
+};
+
+// Accessor over global arrays around linear index s (used for halo cells that
+// are computed at their periodic image).
+template <typename R>
+struct GlobalAcc {
+  const R* f[6];
+  const R* const* b0;
+  long long s, dj, dk;
+  __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
+    const long long o = s + di + djj * dj + dkk * dk;
+    return c >= 6 ? __ldg(b0[c - 6] + o) : __ldg(f[c] + o);
+  }
+  __device__ __forceinline__ R rho(int di, int djj, int dkk) const { return rho_at<R>(*this, di, djj, dkk); }
 };
 
 // ---- PTX helpers: mbarrier + TMA ------------------------------------------
@@ -113,9 +130,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: true when the phase completed
+// bounded wait: true when the phase completed (one probe in the common case)
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-  for (long long it = 0; it < WAIT_LIMIT; ++it)
+  if (__builtin_expect(mbar_try_wait(bar, parity), 1)) return true;
+  for (long long it = 1; it < WAIT_LIMIT; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -150,7 +168,7 @@ struct SmemNew {
   }
 };
 
-template <typename R, bool C, bool B0, bool ABS, bool STAGE1>
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
 __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
   using S = Sizes<R>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -158,24 +176,27 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
   R* en = old + S::OLD;
   R* nw = en + S::EN;
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(nw + S::NEW);
-  const Geom& g = P.g;
+  const Geom g = P.g;
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int kb = blockIdx.z * P.kz;
   const int ke = min(kb + P.kz, g.sz);
   const bool per_x = P.p.bnd[0] == 1, per_y = P.p.bnd[1] == 1, per_z = P.p.bnd[2] == 1;
-  constexpr bool FD = FFE_FAST && !C && sizeof(R) == 4;
+  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  const R cc = P.cc, c1 = P.c1, c2 = P.c2, c3 = P.c3, ct = P.ct;
+  const bool incr = P.incr != 0;
+  R* out[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) out[c] = P.out[c];
 
   const unsigned bar_old = smem_u32(bars), bar_en = smem_u32(bars + DO);
-  // plane p of OLD is use m = p - (kb-2) of slot m % DO; EN: m = p - (kb-1), slot m % DE
-  auto old_slot = [&](int p) { return (p - (kb - 2)) % DO; };
-  auto old_par = [&](int p) { return (unsigned)(((p - (kb - 2)) / DO) & 1); };
-  auto en_slot = [&](int p) { return (p - (kb - 1)) % DE; };
-  auto en_par = [&](int p) { return (unsigned)(((p - (kb - 1)) / DE) & 1); };
-  auto new_slot = [&](int p) { return (p - (kb - 1)) % DN; };
 
-  auto issue_old = [&](int p) {  // one thread
-    const int s = old_slot(p);
+  // ---- producer (thread 0): TMA copies of whole planes --------------------
+  // OLD plane p lives in slot (p - kb + 2) % DO, EN plane p in (p - kb + 1) % DE.
+  int old_next = kb - 2, en_next = kb - 1;
+  const int old_last = ke + 1, en_last = ke;
+  auto issue_old = [&](int p) {
+    const int s = (p - kb + 2) % DO;
     const unsigned bar = bar_old + 8 * s;
     mbar_expect_tx(bar, 6u * OW * OH * sizeof(R));
 #pragma unroll
@@ -183,28 +204,24 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
       tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), &maps.in[c], x0, y0, p + NG, bar);
   };
   auto issue_en = [&](int p) {
-    const int s = en_slot(p);
+    const int s = (p - kb + 1) % DE;
     const unsigned bar = bar_en + 8 * s;
     mbar_expect_tx(bar, 6u * OW * EH * sizeof(R));
 #pragma unroll
     for (int c = 0; c < 6; ++c)
       tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), &maps.en[c], x0, y0 + 1, p + NG, bar);
   };
-
   if (tid == 0) {
     for (int s = 0; s < DO + DE; ++s) mbar_init(smem_u32(bars + s), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb (never past the last plane used)
-  int old_next = kb - 2, en_next = kb - 1;
-  const int old_last = ke + 1, en_last = ke;
-  if (tid == 0) {
+  if (tid == 0) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
     for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
     if (!STAGE1)
       for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
   }
-  // At the top of iteration k, every thread has finished compute_new(k): the
+  // At the top of iteration k every thread has finished compute_new(k): the
   // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
   // may run to k+4 and EN to k+2.
   auto refill = [&](int k) {
@@ -213,9 +230,21 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
     if (!STAGE1)
       while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
   };
-  auto wait_planes = [&](int p_old, int p_en) {
-    bool ok = mbar_wait(bar_old + 8 * old_slot(p_old), old_par(p_old));
-    if (!STAGE1) ok = ok && mbar_wait(bar_en + 8 * en_slot(p_en), en_par(p_en));
+
+  // ---- consumers: rolling ring state, uniform across the block ------------
+  // Planes are waited for in order, each exactly once.
+  int ow_slot = 0;         // slot of the next OLD plane to wait for (kb-2 first)
+  unsigned ow_par = 0;     // its phase parity
+  int ew = 0;              // EN planes waited so far (kb-1 first)
+  auto wait_old = [&]() {
+    const bool ok = mbar_wait(bar_old + 8 * ow_slot, ow_par);
+    if (++ow_slot == DO) { ow_slot = 0; ow_par ^= 1u; }
+    return ok;
+  };
+  auto wait_en = [&]() {
+    if (STAGE1) return true;
+    const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1));
+    ++ew;
     return ok;
   };
 
@@ -223,43 +252,94 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
   const int nxl = tid % NX, nyl = tid / NX;  // NEW cell of this thread (tid < NCELL)
   const int gi = x0 - 1 + nxl, gj = y0 - 1 + nyl;
   const bool xy_in = tid < NCELL && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
+  const bool out_x = gi < 0 || gi >= g.sx, out_y = gj < 0 || gj >= g.sy;
   const bool out_xy_open = ((gi < 0 || gi >= g.sx) && !per_x) || ((gj < 0 || gj >= g.sy) && !per_y);
-  const int toff_old = (nyl + 1) * OW + (nxl + 1);  // this cell in an OLD box
-  const int toff_en = nyl * OW + (nxl + 1);         // in an EN box
-  const int toff_new = nyl * NX + nxl;              // in a NEW plane
+  const R* oth = old + (nyl + 1) * OW + (nxl + 1);  // this cell in OLD slot 0
+  const R* enth = en + nyl * OW + (nxl + 1);        // in EN slot 0
+  R* nwth = nw + nyl * NX + nxl;                    // in NEW slot 0
   long long gbase = 0;
   if (B0 && xy_in) gbase = g.idx(gi, gj, 0);
+  // the whole 34x10 region lies in [-1, s] and needs no frozen ghost in x, y
+  const bool simple_xy = x0 + TX <= g.sx && y0 + TY <= g.sy &&
+                         (per_x || (x0 >= 1 && x0 + TX + 1 <= g.sx)) &&
+                         (per_y || (y0 >= 1 && y0 + TY + 1 <= g.sy));
+  // periodic and open axes together: edge tiles and edge planes go cell by cell
+  const bool mixed = (per_x || per_y || per_z) && !(per_x && per_y && per_z);
+  const bool edge_xy = x0 == 0 || x0 + TX >= g.sx || y0 == 0 || y0 + TY >= g.sy;
+  // no cell of the tile has a periodic image in x or y
+  const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
+                            (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
 
-  auto compute_new = [&](int p) {
+  // NEW(p): push + update on this thread's cell.  so = OLD slot of plane p-1,
+  // m = p - (kb - 1) (EN slot m % 2, NEW slot m % 4).
+  auto compute_new = [&](int p, int so, int m) {
     if (tid >= NCELL) return;
-    R* dst = nw + new_slot(p) * 6 * S::NEWPL + toff_new;
-    const R* o1 = old + old_slot(p) * 6 * S::OLDBOX + toff_old;
+    const int s1 = so == DO - 1 ? 0 : so + 1;
+    const int s2 = s1 == DO - 1 ? 0 : s1 + 1;
+    const R* o1 = oth + s1 * (6 * S::OLDBOX);
+    R* dst = nwth + (m & (DN - 1)) * (6 * S::NEWPL);
     R v[6];
-    const bool in_range = xy_in && p >= -1 && p <= g.sz;
-    const bool frozen = out_xy_open || ((p < 0 || p >= g.sz) && !per_z);
-    if (!in_range) {
+    // block-uniform common case: every cell of the region is computed
+    const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
+                          !(mixed && (edge_xy || p <= 0 || p >= g.sz - 1));
+    bool push = true;
+    if (!all_push) {
+      const bool in_range = xy_in && p >= -1 && p <= g.sz;
+      const bool out_z = p < 0 || p >= g.sz;
+      const bool frozen = out_xy_open || (out_z && !per_z);
+      if (!in_range || frozen) {
 #pragma unroll
-      for (int c = 0; c < 6; ++c) v[c] = R(0);
-    } else if (frozen) {
+        for (int c = 0; c < 6; ++c) v[c] = in_range ? o1[c * S::OLDBOX] : R(0);
+        push = false;
+      } else if (out_x || out_y || out_z) {
+        // A halo cell outside a periodic face is the periodic image of an
+        // interior cell.  If that cell lies next to an open face, its stencil
+        // reaches ghosts of the open face at positions whose counterparts here
+        // are ghosts of both faces, which keep their own (frozen) values: the
+        // copy at this position would differ.  Compute it at the image instead.
+        const int wi = gi < 0 ? gi + g.sx : (gi >= g.sx ? gi - g.sx : gi);
+        const int wj = gj < 0 ? gj + g.sy : (gj >= g.sy ? gj - g.sy : gj);
+        const int wk = p < 0 ? p + g.sz : (p >= g.sz ? p - g.sz : p);
+        const bool near_open = (!per_x && (wi == 0 || wi == g.sx - 1)) || (!per_y && (wj == 0 || wj == g.sy - 1)) ||
+                               (!per_z && (wk == 0 || wk == g.sz - 1));
+        if (near_open) {
+          GlobalAcc<R> a;
+          for (int c = 0; c < 6; ++c) a.f[c] = P.in_g[c];
+          a.b0 = P.b0;
+          a.s = g.idx(wi, wj, wk);
+          a.dj = g.px;
+          a.dk = g.plane;
+          R d[6];
+          if constexpr (FD) push_cell_fast<B0>(a, cc, d);
+          else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) v[c] = o1[c * S::OLDBOX];
-    } else {
+          for (int c = 0; c < 6; ++c) {
+            const R f = __ldg(P.in_g[c] + a.s);
+            const R fn = STAGE1 ? f : __ldg(P.en_g[c] + a.s);
+            v[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
+          }
+          push = false;
+        }
+      }
+    }
+    if (push) {
       SmemOld<R> a;
-      a.b[0] = old + old_slot(p - 1) * 6 * S::OLDBOX + toff_old;
+      a.b[0] = oth + so * (6 * S::OLDBOX);
       a.b[1] = o1;
-      a.b[2] = old + old_slot(p + 1) * 6 * S::OLDBOX + toff_old;
+      a.b[2] = oth + s2 * (6 * S::OLDBOX);
       a.b0 = P.b0;
       a.gs = gbase + (long long)p * g.plane;
       a.dj = g.px;
       a.dk = g.plane;
       R d[6];
-      push_cell<R, C, B0, SmemOld<R>, FD>(a, P.cc, d);
-      const R* e1 = STAGE1 ? o1 : en + en_slot(p) * 6 * S::ENBOX + toff_en;
+      if constexpr (FD) push_cell_fast<B0>(a, cc, d);
+      else push_cell<R, C, B0, SmemOld<R>, false>(a, cc, d);
+      const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         const R f = o1[c * S::OLDBOX];
         const R fn = STAGE1 ? f : e1[c * S::ENBOX];
-        v[c] = combine<R, C>(P.c1, P.c2, P.c3, fn, f, d[c], P.incr != 0);
+        v[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
       if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, gi + P.p.y0, p + P.p.z0, v);
     }
@@ -278,22 +358,25 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
   if (per_y && cj < NG) ys[nys++] = cj + g.sy;
   if (per_y && cj >= g.sy - NG) ys[nys++] = cj - g.sy;
   const bool xy_images = nxs > 1 || nys > 1;
-  const int toff_c = (ly + 1) * NX + (lx + 1);
+  const R* cth = nw + (ly + 1) * NX + (lx + 1);
+  const long long cbase = c_in ? g.idx(ci, cj, 0) : 0;
 
-  auto clean_store = [&](int k) {
+  // clean plane k (m = k - kb: NEW slots of k-1, k, k+1 are m, m+1, m+2 mod 4)
+  auto clean_store = [&](int k, int m) {
     if (!c_in) return;
     SmemNew<R> a;
-    a.b[0] = nw + new_slot(k - 1) * 6 * S::NEWPL + toff_c;
-    a.b[1] = nw + new_slot(k) * 6 * S::NEWPL + toff_c;
-    a.b[2] = nw + new_slot(k + 1) * 6 * S::NEWPL + toff_c;
+    a.b[0] = cth + (m & (DN - 1)) * (6 * S::NEWPL);
+    a.b[1] = cth + ((m + 1) & (DN - 1)) * (6 * S::NEWPL);
+    a.b[2] = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
     R e[3];
-    clean_cell<R, C, SmemNew<R>, FD>(a, e, P.ct);
+    if constexpr (FD) clean_cell_fast(a, e, ct);
+    else clean_cell<R, C, SmemNew<R>, false>(a, e, ct);
     const R v[6] = {e[0], e[1], e[2], a(BX, 0, 0, 0), a(BY, 0, 0, 0), a(BZ, 0, 0, 0)};
     const bool z_image = per_z && (k < NG || k >= g.sz - NG);
-    if (!xy_images && !z_image) {
-      const long long o = g.idx(ci, cj, k);
+    if ((no_xy_images || !xy_images) && !z_image) {
+      const long long o = cbase + (long long)k * g.plane;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) P.out[c][o] = v[c];
+      for (int c = 0; c < 6; ++c) out[c][o] = v[c];
       return;
     }
     int zs[3] = {k, k, k}, nzs = 1;
@@ -304,25 +387,27 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
         for (int a0 = 0; a0 < nxs; ++a0) {
           const long long o = g.idx(xs[a0], ys[a1], zs[a2]);
 #pragma unroll
-          for (int c = 0; c < 6; ++c) P.out[c][o] = v[c];
+          for (int c = 0; c < 6; ++c) out[c][o] = v[c];
         }
   };
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
-  bool failed = !wait_planes(kb - 2, kb - 1) || !wait_planes(kb - 1, kb - 1) || !wait_planes(kb, kb - 1);
+  bool failed = !(wait_old() & wait_old() & wait_old() & wait_en());  // OLD kb-2..kb, EN kb-1
   if (!__syncthreads_or(failed)) {
-    compute_new(kb - 1);
-    failed = !wait_planes(kb + 1, kb);
+    compute_new(kb - 1, 0, 0);
+    failed = !(wait_old() & wait_en());  // OLD kb+1, EN kb
     if (!__syncthreads_or(failed)) {
-      compute_new(kb);
+      compute_new(kb, 1, 1);
       __syncthreads();
       // ---- march: one barrier per plane ------------------------------------
-      for (int k = kb; k < ke; ++k) {
+      int so = 2;  // OLD slot of plane k for compute_new(k+1)
+      for (int k = kb, m = 0; k < ke; ++k, ++m) {
         refill(k);
-        failed = !wait_planes(k + 2, k + 1);
-        if (!failed) compute_new(k + 1);
+        failed = !(wait_old() & wait_en());  // OLD k+2, EN k+1
+        if (!failed) compute_new(k + 1, so, m + 2);
         if (__syncthreads_or(failed)) break;
-        clean_store(k);
+        clean_store(k, m);
+        so = so == DO - 1 ? 0 : so + 1;
       }
     }
   }
@@ -330,12 +415,145 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
     if (tid == 0) {
       atomicExch(P.err, 1);
       // drain the copies that may still be in flight: the last use of each slot
-      for (int p = max(kb - 2, old_next - DO); p < old_next; ++p) mbar_wait(bar_old + 8 * old_slot(p), old_par(p));
+      for (int p = max(kb - 2, old_next - DO); p < old_next; ++p)
+        mbar_wait(bar_old + 8 * ((p - kb + 2) % DO), (unsigned)(((p - kb + 2) / DO) & 1));
       if (!STAGE1)
-        for (int p = max(kb - 1, en_next - DE); p < en_next; ++p) mbar_wait(bar_en + 8 * en_slot(p), en_par(p));
+        for (int p = max(kb - 1, en_next - DE); p < en_next; ++p)
+          mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1));
     }
     __syncthreads();
   }
+}
+
+// ---- rotating-conductor boundary condition on the fused path ---------------
+// The fused kernel cleans every cell before any boundary condition could act.
+// For the pulsar setup the BC (user/user_psr.F90:72-332) modifies the cells of
+// its bounding box B between the update and the cleaning, and the cleaning of
+// a cell reads its neighbours, so the cells of B+1 (B dilated by one cell) are
+// redone after the fused launch:
+//   k_fix_update: uncleaned update (push + combine [+ shell]) on U = B+2 -> S1
+//   k_fix_bc:     S2 = S1 with the BC applied inside r < 2R (reads S1 neighbours)
+//   k_fix_clean:  clean the interior cells of B+1 from S2, store E'' and B'
+// S1, S2 are compact U-shaped arrays (6 components).  Only for grids with no
+// periodic axis (the pulsar runs open or absorbing), so U holds no image.
+template <typename R>
+struct FixParams {
+  Geom g;
+  Phys p;
+  Absorb<R> ab;
+  PsrBC<R> q;
+  R cc, c1, c2, c3, ct;
+  int incr;
+  int ui, uj, uk, ux, uy, uz;  // U: first cell and extents
+  const R* in[6];
+  const R* en[6];
+  const R* b0[3];
+  R* out[6];
+  R* s1;
+  R* s2;
+};
+
+template <typename R>
+struct BoxAcc {  // accessor over a compact U array around a cell
+  const R* base;
+  long long n, s, dj, dk;
+  __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
+    return base[c * n + s + di + djj * dj + dkk * dk];
+  }
+};
+
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
+__global__ void k_fix_update(const FixParams<R> F) {
+  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x, bj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int bk = blockIdx.z;
+  if (bi >= F.ux || bj >= F.uy) return;
+  const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
+  const Geom& g = F.g;
+  const long long n = (long long)F.ux * F.uy * F.uz;
+  const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
+  const long long s = g.idx(i, j, k);
+  R v[6];
+  if (i < 0 || i >= g.sx || j < 0 || j >= g.sy || k < 0 || k >= g.sz) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = __ldg(F.in[c] + s);  // frozen ghost
+  } else {
+    GlobalAcc<R> a;
+    for (int c = 0; c < 6; ++c) a.f[c] = F.in[c];
+    a.b0 = F.b0;
+    a.s = s;
+    a.dj = g.px;
+    a.dk = g.plane;
+    R d[6];
+    if constexpr (FD) push_cell_fast<B0>(a, F.cc, d);
+    else push_cell<R, C, B0, GlobalAcc<R>, false>(a, F.cc, d);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const R f = __ldg(F.in[c] + s);
+      const R fn = STAGE1 ? f : __ldg(F.en[c] + s);
+      v[c] = combine<R, C>(F.c1, F.c2, F.c3, fn, f, d[c], F.incr != 0);
+    }
+    if (ABS) absorb_cell<R>(F.ab, i + F.p.x0, i + F.p.y0, k + F.p.z0, v);
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) F.s1[c * n + o] = v[c];
+}
+
+template <typename R>
+__global__ void k_fix_bc(const FixParams<R> F) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x, bj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int bk = blockIdx.z;
+  if (bi >= F.ux || bj >= F.uy) return;
+  const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
+  const long long n = (long long)F.ux * F.uy * F.uz;
+  const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
+  const bool in_b = i >= F.q.i_lo && i <= F.q.i_hi && j >= F.q.j_lo && j <= F.q.j_hi && k >= F.q.k_lo &&
+                    k <= F.q.k_hi;
+  if (in_b && psr_inside(F.q, F.p, i, j, k)) {
+    BoxAcc<R> a;
+    a.base = F.s1;
+    a.n = n;
+    a.s = o;
+    a.dj = F.ux;
+    a.dk = (long long)F.ux * F.uy;
+    R v[6];
+    psr_cell(F.q, F.p, a, i, j, k, v);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F.s2[c * n + o] = v[c];
+  } else {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F.s2[c * n + o] = F.s1[c * n + o];
+  }
+}
+
+template <typename R, int C>
+__global__ void k_fix_clean(const FixParams<R> F) {
+  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  // cells of B+1 = U shrunk by one on every side, interior only
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x + 1, bj = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int bk = blockIdx.z + 1;
+  if (bi >= F.ux - 1 || bj >= F.uy - 1) return;
+  const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
+  const Geom& g = F.g;
+  if (i < 0 || i >= g.sx || j < 0 || j >= g.sy || k < 0 || k >= g.sz) return;
+  const long long n = (long long)F.ux * F.uy * F.uz;
+  const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
+  BoxAcc<R> a;
+  a.base = F.s2;
+  a.n = n;
+  a.s = o;
+  a.dj = F.ux;
+  a.dk = (long long)F.ux * F.uy;
+  R e[3];
+  if constexpr (FD) clean_cell_fast(a, e, F.ct);
+  else clean_cell<R, C, BoxAcc<R>, false>(a, e, F.ct);
+  const long long s = g.idx(i, j, k);
+  F.out[0][s] = e[0];
+  F.out[1][s] = e[1];
+  F.out[2][s] = e[2];
+  F.out[3][s] = a(BX, 0, 0, 0);
+  F.out[4][s] = a(BY, 0, 0, 0);
+  F.out[5][s] = a(BZ, 0, 0, 0);
 }
 
 }  // namespace FFE_FUSED_NS
@@ -346,10 +564,10 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
 #define FFE_LAUNCH_NAME launch_fused_stage
 #endif
 
-template <typename R, bool C>
+template <typename R, int C>
 int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
-                    const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
-                    int* err, cudaStream_t st) {
+                    const void* maps_in, const void* maps_en, const CEB<R>& in_g, const CEB<R>& en_g,
+                    const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err, cudaStream_t st) {
   using namespace FFE_FUSED_NS;
   Maps M;
   memcpy(M.in, maps_in, sizeof(M.in));
@@ -366,6 +584,10 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.incr = incr ? 1 : 0;
   for (int c = 0; c < 6; ++c) P.out[c] = out.c[c];
   for (int c = 0; c < 3; ++c) P.b0[c] = b0.c[c];
+  for (int c = 0; c < 6; ++c) {
+    P.in_g[c] = in_g.c[c];
+    P.en_g[c] = en_g.c[c];
+  }
   P.err = err;
   const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
   // enough blocks for ~16 per SM on 152 SMs, at least 8 planes per block
@@ -397,6 +619,66 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
     else { if (s1) FFE_GO(false, false, true); else FFE_GO(false, false, false); }
   }
 #undef FFE_GO
+  return 0;
+}
+
+#ifdef FFE_FUSED_EXACT
+#define FFE_FIX_NAME launch_psr_fixup_exact
+#else
+#define FFE_FIX_NAME launch_psr_fixup
+#endif
+
+// U = the pulsar BC's bounding box dilated by two cells, clipped to the array.
+static void psr_fix_box(const Geom& g, int i_lo, int i_hi, int j_lo, int j_hi, int k_lo, int k_hi, int u[6]) {
+  u[0] = std::max(-NG, i_lo - 2);
+  u[1] = std::max(-NG, j_lo - 2);
+  u[2] = std::max(-NG, k_lo - 2);
+  u[3] = std::min(g.sx + NG - 1, i_hi + 2) - u[0] + 1;
+  u[4] = std::min(g.sy + NG - 1, j_hi + 2) - u[1] + 1;
+  u[5] = std::min(g.sz + NG - 1, k_hi + 2) - u[2] + 1;
+}
+
+template <typename R, int C>
+int FFE_FIX_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<R>& q, R cc, R c1, R c2, R c3,
+                 bool incr, int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0,
+                 const EB<R>& out, R ct, R* s1, R* s2, cudaStream_t st) {
+  using namespace FFE_FUSED_NS;
+  if (q.bx <= 0 || q.by <= 0 || q.bz <= 0) return 0;
+  FixParams<R> F;
+  F.g = g;
+  F.p = p;
+  F.ab = ab;
+  F.q = q;
+  F.cc = cc;
+  F.c1 = c1;
+  F.c2 = c2;
+  F.c3 = c3;
+  F.ct = ct;
+  F.incr = incr ? 1 : 0;
+  int u[6];
+  psr_fix_box(g, q.i_lo, q.i_hi, q.j_lo, q.j_hi, q.k_lo, q.k_hi, u);
+  F.ui = u[0]; F.uj = u[1]; F.uk = u[2]; F.ux = u[3]; F.uy = u[4]; F.uz = u[5];
+  for (int c = 0; c < 6; ++c) {
+    F.in[c] = in.c[c];
+    F.en[c] = en.c[c];
+    F.out[c] = out.c[c];
+  }
+  for (int c = 0; c < 3; ++c) F.b0[c] = b0.c[c];
+  F.s1 = s1;
+  F.s2 = s2;
+  const dim3 b(32, 8, 1), gr((F.ux + 31) / 32, (F.uy + 7) / 8, F.uz);
+  const bool abs = p.bnd[0] == 2, s1st = stage == 1;
+#define FFE_FIXGO(B0V, ABSV, S1V) k_fix_update<R, C, B0V, ABSV, S1V><<<gr, b, 0, st>>>(F)
+  if (has_b0) {
+    if (abs) { if (s1st) FFE_FIXGO(true, true, true); else FFE_FIXGO(true, true, false); }
+    else { if (s1st) FFE_FIXGO(true, false, true); else FFE_FIXGO(true, false, false); }
+  } else {
+    if (abs) { if (s1st) FFE_FIXGO(false, true, true); else FFE_FIXGO(false, true, false); }
+    else { if (s1st) FFE_FIXGO(false, false, true); else FFE_FIXGO(false, false, false); }
+  }
+#undef FFE_FIXGO
+  k_fix_bc<R><<<gr, b, 0, st>>>(F);
+  k_fix_clean<R, C><<<gr, b, 0, st>>>(F);
   return 0;
 }
 
@@ -436,10 +718,19 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
 
 #define FFE_INST_F(R, C)                                                                                        \
   template int FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,        \
-                                     const void*, const void*, const CEB<R>&, bool, const EB<R>&, R, int*,      \
-                                     cudaStream_t);
-FFE_INST_F(float, false)
-FFE_INST_F(float, true)
-FFE_INST_F(double, false)
+                                     const void*, const void*, const CEB<R>&, const CEB<R>&, const CEB<R>&,     \
+                                     bool, const EB<R>&, R, int*, cudaStream_t);
+#define FFE_INST_X(R, C)                                                                                        \
+  template int FFE_FIX_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, const PsrBC<R>&, R, R, R, R, bool, \
+                                  int, const CEB<R>&, const CEB<R>&, const CEB<R>&, bool, const EB<R>&, R, R*,   \
+                                  R*, cudaStream_t);
+FFE_INST_F(float, 0)
+FFE_INST_F(float, 1)
+FFE_INST_F(float, 2)
+FFE_INST_F(double, 0)
+FFE_INST_X(float, 0)
+FFE_INST_X(float, 1)
+FFE_INST_X(float, 2)
+FFE_INST_X(double, 0)
 
 }  // namespace ffe

@@ -9,13 +9,13 @@ namespace ffe {
 // ---- staged kernels (ffe_staged.cu), one per reference procedure -----------
 template <typename R>
 void launch_rho(const Geom& g, const R* ex, const R* ey, const R* ez, R* rho, cudaStream_t st);
-template <typename R, bool C>
+template <typename R, int C>
 void launch_push(const Geom& g, R cc, const CEB<R>& eb, const CEB<R>& b0, bool has_b0, const R* rho, const EB<R>& d,
                  cudaStream_t st);
-template <typename R, bool C>
+template <typename R, int C>
 void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2, R c3, bool incr, const EB<R>& f,
                    const CEB<R>& fn, const CEB<R>& df, cudaStream_t st);
-template <typename R, bool C>
+template <typename R, int C>
 void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStream_t st);
 template <typename R>
 void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st);
@@ -48,14 +48,28 @@ void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
 // step-start set) made by make_stage_maps; err: device word set on a timeout.
 // Returns 0, or -3 if the kernel attribute could not be set.
 // ct: TINY added to the cleaning denominators (FFE_FLAG_CLEAN_TINY) or 0.
-template <typename R, bool C>
+// in_g / en_g: the same two sets as plain pointers (for halo cells computed at
+// their periodic image next to an open face).
+template <typename R, int C>
 int launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
-                       int stage, const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0,
-                       const EB<R>& out, R ct, int* err, cudaStream_t st);
-template <typename R, bool C>
+                       int stage, const void* maps_in, const void* maps_en, const CEB<R>& in_g, const CEB<R>& en_g,
+                       const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err, cudaStream_t st);
+template <typename R, int C>
 int launch_fused_stage_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
-                             int stage, const void* maps_in, const void* maps_en, const CEB<R>& b0, bool has_b0,
-                             const EB<R>& out, R ct, int* err, cudaStream_t st);
+                             int stage, const void* maps_in, const void* maps_en, const CEB<R>& in_g,
+                             const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err,
+                             cudaStream_t st);
+// Pulsar BC on the fused path: after a fused stage, redo the cells of the BC's
+// bounding box dilated by one (update on box+2 into s1, BC into s2, clean into
+// out).  s1, s2: 6 * (bx+4)(by+4)(bz+4) elements each.
+template <typename R, int C>
+int launch_psr_fixup(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<R>& q, R cc, R c1, R c2, R c3,
+                     bool incr, int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0, bool has_b0,
+                     const EB<R>& out, R ct, R* s1, R* s2, cudaStream_t st);
+template <typename R, int C>
+int launch_psr_fixup_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<R>& q, R cc, R c1, R c2,
+                           R c3, bool incr, int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0,
+                           bool has_b0, const EB<R>& out, R ct, R* s1, R* s2, cudaStream_t st);
 // The two TMA tensor maps (OLD box, EN box) of one field array at `base`.
 int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es);
 // Tile shape the fused kernel uses (for reporting).

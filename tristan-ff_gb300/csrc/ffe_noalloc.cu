@@ -66,7 +66,7 @@ struct RefAcc {  // neighbours in a caller's (sx+4)(sy+4)(sz+4) array
 };
 
 // cleanEpar of one interior cell into the compact scratch (3 x sx*sy*sz).
-template <typename R, bool C>
+template <typename R, int C>
 __global__ void k_clean_noalloc(Geom g, CEB<R> eb, R* __restrict__ scratch) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -102,7 +102,7 @@ __global__ void k_copy_noalloc(Geom g, const R* __restrict__ scratch, R* __restr
   ez[s] = scratch[2 * n + o];
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 int run(const Geom& g, void* ex, void* ey, void* ez, const void* bx, const void* by, const void* bz, void* scratch,
         cudaStream_t st) {
   CEB<R> eb;
@@ -124,7 +124,7 @@ extern "C" int ffe_clean_epar_noalloc(int32_t sx, int32_t sy, int32_t sz, int32_
   using namespace ffe;
   if (sx < FFE_NGHOST || sy < FFE_NGHOST || sz < FFE_NGHOST)
     return set_thread_error(FFE_EINVAL, "clean_epar_noalloc: each size must be >= 2 (NGHOST)");
-  if (precision < FFE_FP64 || precision > FFE_FP32C)
+  if (precision < FFE_FP64 || precision > FFE_FP32CD)
     return set_thread_error(FFE_EINVAL, "clean_epar_noalloc: bad precision");
   if (!ex || !ey || !ez || !bx || !by || !bz) return set_thread_error(FFE_EINVAL, "clean_epar_noalloc: null array");
   const size_t es = precision == FFE_FP64 ? 8 : 4;
@@ -144,7 +144,7 @@ extern "C" int ffe_clean_epar_noalloc(int32_t sx, int32_t sy, int32_t sz, int32_
   g.plane = (long long)g.px * g.py;
   g.nelem = g.plane * (sz + 2 * FFE_NGHOST);
   cudaStream_t st = (cudaStream_t)stream;
-  if (precision == FFE_FP64) return run<double, false>(g, ex, ey, ez, bx, by, bz, scratch, st);
-  if (precision == FFE_FP32C) return run<float, true>(g, ex, ey, ez, bx, by, bz, scratch, st);
-  return run<float, false>(g, ex, ey, ez, bx, by, bz, scratch, st);
+  if (precision == FFE_FP64) return run<double, 0>(g, ex, ey, ez, bx, by, bz, scratch, st);
+  if (precision == FFE_FP32CD) return run<float, 2>(g, ex, ey, ez, bx, by, bz, scratch, st);
+  return run<float, 0>(g, ex, ey, ez, bx, by, bz, scratch, st);  // FP32, FP32C: same cleaning
 }

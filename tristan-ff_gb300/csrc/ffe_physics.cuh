@@ -36,9 +36,9 @@ __device__ __forceinline__ R qdiv(R x, R y) {
 }
 
 // J = CC rho (E x B) / (B^2 + TINY) with the denominator in R, or in double (FP32C).
-template <typename R, bool C, bool FD = false>
+template <typename R, int C, bool FD = false>
 __device__ __forceinline__ R jdiv(R cc, R bmag, R bx, R by, R bz, R num) {
-  if (C) {
+  if (C == 2) {
     const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
     return (R)((double)cc / (bd + (double)tiny<float>()) * (double)num);
   }
@@ -46,7 +46,7 @@ __device__ __forceinline__ R jdiv(R cc, R bmag, R bx, R by, R bz, R num) {
 }
 
 // rk3Push (field_solver.F90:81-162): writes dE (with -J) and dB of one cell.
-template <typename R, bool C, bool B0, class A, bool FD = false>
+template <typename R, int C, bool B0, class A, bool FD = false>
 __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
   const R ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -126,7 +126,7 @@ __device__ __forceinline__ void push_cell(const A& a, R cc, R d[6]) {
 
 // RK combination (field_solver.F90:187-193): (c1*fn + c2*f) + c3*df, or the
 // FP32C increment form fn + (c2*(f - fn) + c3*df), used when c1 + c2 == 1.
-template <typename R, bool C>
+template <typename R, int C>
 __device__ __forceinline__ R combine(R c1, R c2, R c3, R fn, R f, R df, bool incr) {
   if (C && incr) return fn + (c2 * (f - fn) + c3 * df);
   return (c1 * fn + c2 * f) + c3 * df;
@@ -156,17 +156,17 @@ __device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int j
 }
 
 // cleanEpar (field_solver.F90:288-328): E - (E.B) B / B^2 at the three E points.
-template <typename R, bool C, bool FD = false>
+template <typename R, int C, bool FD = false>
 __device__ __forceinline__ R clean_div(R epar, R bi, R bmag, R bx, R by, R bz, R ct) {
   // ct = 0 (the reference) or TINY (FFE_FLAG_CLEAN_TINY); bmag + 0 == bmag exactly
-  if (C) {
+  if (C == 2) {
     const double bd = ((double)bx * (double)bx + (double)by * (double)by) + (double)bz * (double)bz;
     return (R)((double)(epar * bi) / (bd + (double)ct));
   }
   return qdiv<R, FD>(epar * bi, bmag + ct);
 }
 
-template <typename R, bool C, class A, bool FD = false>
+template <typename R, int C, class A, bool FD = false>
 __device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
   const R ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const R bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -203,6 +203,115 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
   bmag = (intbx * intbx + intby * intby) + intbz * intbz;
   epar = (intex * intbx + intey * intby) + intez * intbz;
   e[2] = ez0 - clean_div<R, C, FD>(epar, intbz, bmag, intbx, intby, intbz, ct);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 fast-path forms of push_cell / clean_cell.  The reference averages are
+// sums times 1/2, 1/4 or 1/8; those power-of-two factors are moved out of the
+// products and gathered into one constant per quotient, which is exact in
+// binary arithmetic (no rounding changes, barring subnormals) and removes
+// about a dozen multiplies per cell.  With S the bare sums:
+//   64 B^2 = S8^2 + 16 (S2a^2 + S2b^2),   64 E^2 = 64 e0^2 + 4 (S4a^2 + S4b^2),
+//   J_i    = 4 CC / (64 B^2 + 64 TINY) * Srho * (cross product of bare sums),
+//   clean:   E_i -= (S.B-sums dot) * S8 / (64 B^2 + 64 ct).
+// ---------------------------------------------------------------------------
+template <class A>
+__device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, float s4a, float s4b,
+                                              float s8, float s2a, float s2b, float& ea, float& eb) {
+  const float bm = s8 * s8 + 16.f * (s2a * s2a + s2b * s2b);
+  const float em = 64.f * (e0 * e0) + 4.f * (s4a * s4a + s4b * s4b);
+  // limiter as a select: corr = 1 leaves the values unchanged exactly
+  const float corr = em > bm ? sqrtf(__fdividef(bm, em)) : 1.f;
+  ea = s4a * corr;
+  eb = s4b * corr;
+  return __fdividef(cc4, bm + t64) * sr;
+}
+
+template <bool B0, class A>
+__device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6]) {
+  const float ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
+  const float bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
+  d[3] = cc * ((a(EY, 0, 0, 1) - ey0) - (a(EZ, 0, 1, 0) - ez0));
+  d[4] = cc * ((a(EZ, 1, 0, 0) - ez0) - (a(EX, 0, 0, 1) - ex0));
+  d[5] = cc * ((a(EX, 0, 1, 0) - ex0) - (a(EY, 1, 0, 0) - ey0));
+  float cbx = (by0 - a(BY, 0, 0, -1)) - (bz0 - a(BZ, 0, -1, 0));
+  float cby = (bz0 - a(BZ, -1, 0, 0)) - (bx0 - a(BX, 0, 0, -1));
+  float cbz = (bx0 - a(BX, 0, -1, 0)) - (by0 - a(BY, -1, 0, 0));
+  if (B0) {
+    cbx = cbx - ((a(B0Y, 0, 0, 0) - a(B0Y, 0, 0, -1)) - (a(B0Z, 0, 0, 0) - a(B0Z, 0, -1, 0)));
+    cby = cby - ((a(B0Z, 0, 0, 0) - a(B0Z, -1, 0, 0)) - (a(B0X, 0, 0, 0) - a(B0X, 0, 0, -1)));
+    cbz = cbz - ((a(B0X, 0, 0, 0) - a(B0X, 0, -1, 0)) - (a(B0Y, 0, 0, 0) - a(B0Y, -1, 0, 0)));
+  }
+  const float r0 = a.rho(0, 0, 0);
+  const float cc4 = 4.f * cc, t64 = 64.f * tiny<float>();
+  float ea, eb, k;
+  // X current at the Ex point (field_solver.F90:91-111)
+  {
+    const float sy = ((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0);
+    const float sz = ((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1);
+    const float b8 = ((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
+                       a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1);
+    const float by2 = by0 + a(BY, 0, 0, -1), bz2 = bz0 + a(BZ, 0, -1, 0);
+    k = fast_current<A>(cc4, t64, a.rho(1, 0, 0) + r0, ex0, sy, sz, b8, by2, bz2, ea, eb);
+    d[0] = -(cc * cbx) - k * (ea * bz2 - by2 * eb);
+  }
+  // Y current at the Ey point (:114-134)
+  {
+    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0);
+    const float sz = ((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1);
+    const float b8 = ((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
+                       a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1);
+    const float bx2 = bx0 + a(BX, 0, 0, -1), bz2 = bz0 + a(BZ, -1, 0, 0);
+    k = fast_current<A>(cc4, t64, a.rho(0, 1, 0) + r0, ey0, sx, sz, b8, bx2, bz2, ea, eb);
+    d[1] = -(cc * cby) - k * (eb * bx2 - ea * bz2);
+  }
+  // Z current at the Ez point (:137-157)
+  {
+    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1);
+    const float sy = ((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1);
+    const float b8 = ((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
+                       a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1);
+    const float bx2 = bx0 + a(BX, 0, -1, 0), by2 = by0 + a(BY, -1, 0, 0);
+    k = fast_current<A>(cc4, t64, r0 + a.rho(0, 0, 1), ez0, sx, sy, b8, bx2, by2, ea, eb);
+    d[2] = -(cc * cbz) - k * (ea * by2 - bx2 * eb);
+  }
+}
+
+template <class A>
+__device__ __forceinline__ void clean_cell_fast(const A& a, float e[3], float ct) {
+  const float ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
+  const float bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
+  const float c64 = 64.f * ct;
+  {  // Ex point (:289-300)
+    const float sy = ((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0);
+    const float sz = ((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1);
+    const float b8 = ((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
+                       a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1);
+    const float b2a = by0 + a(BY, 0, 0, -1), b2b = bz0 + a(BZ, 0, -1, 0);
+    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
+    const float ep = ex0 * b8 + sy * b2a + sz * b2b;
+    e[0] = ex0 - __fdividef(ep * b8, bm + c64);
+  }
+  {  // Ey point (:303-314)
+    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0);
+    const float sz = ((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1);
+    const float b8 = ((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
+                       a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1);
+    const float b2a = bx0 + a(BX, 0, 0, -1), b2b = bz0 + a(BZ, -1, 0, 0);
+    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
+    const float ep = sx * b2a + ey0 * b8 + sz * b2b;
+    e[1] = ey0 - __fdividef(ep * b8, bm + c64);
+  }
+  {  // Ez point (:317-328)
+    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1);
+    const float sy = ((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1);
+    const float b8 = ((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
+                       a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1);
+    const float b2a = bx0 + a(BX, 0, -1, 0), b2b = by0 + a(BY, -1, 0, 0);
+    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
+    const float ep = sx * b2a + sy * b2b + ez0 * b8;
+    e[2] = ez0 - __fdividef(ep * b8, bm + c64);
+  }
 }
 
 }  // namespace ffe

@@ -9,6 +9,7 @@
 // (transcendentals aside: tanh, exp of the user boundary conditions).
 #include "ffe_kernels.h"
 #include "ffe_physics.cuh"
+#include "ffe_psr.cuh"
 
 namespace ffe {
 
@@ -43,7 +44,7 @@ __global__ void k_rho(Geom g, const R* __restrict__ ex, const R* __restrict__ ey
 }
 
 // ---- rk3Push over the interior (field_solver.F90:78-165) ------------------
-template <typename R, bool C, bool B0>
+template <typename R, int C, bool B0>
 __global__ void k_push(Geom g, R cc, CEB<R> eb, CEB<R> b0, const R* __restrict__ rho, EB<R> d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -62,7 +63,7 @@ __global__ void k_push(Geom g, R cc, CEB<R> eb, CEB<R> b0, const R* __restrict__
 }
 
 // ---- rk3Update over the interior (field_solver.F90:180-268) ---------------
-template <typename R, bool C, bool ABS>
+template <typename R, int C, bool ABS>
 __global__ void k_update(Geom g, Phys p, Absorb<R> ab, R c1, R c2, R c3, int incr, EB<R> f, CEB<R> fn, CEB<R> df) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -78,7 +79,7 @@ __global__ void k_update(Geom g, Phys p, Absorb<R> ab, R c1, R c2, R c3, int inc
 }
 
 // ---- cleanEpar into dE, then dE -> E over the interior (:284-334) ---------
-template <typename R, bool C>
+template <typename R, int C>
 __global__ void k_clean(Geom g, CEB<R> eb, R* __restrict__ dex, R* __restrict__ dey, R* __restrict__ dez, R ct) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -155,69 +156,6 @@ __global__ void k_fill(Geom g, int per_x, int per_y, int per_z, int nf, EB<R> f6
 }
 
 // ---- user_psr boundary condition (user/user_psr.F90:72-332) ---------------
-template <typename R>
-__device__ __forceinline__ void psr_dipole(const PsrBC<R>& q, R x_g, R y_g, R z_g, R& obx, R& oby, R& obz) {
-  R nx = x_g - q.xc, ny = y_g - q.yc, nz = z_g - q.zc;
-  R rr = R(1.0) / sqrt((nx * nx + ny * ny) + nz * nz);
-  nx = nx * rr;
-  ny = ny * rr;
-  nz = nz * rr;
-  rr = (rr * rr) * rr;
-  const R mdn = (q.mu[0] * nx + q.mu[1] * ny) + q.mu[2] * nz;
-  obx = (R(3.0) * nx * mdn - q.mu[0]) * rr;
-  oby = (R(3.0) * ny * mdn - q.mu[1]) * rr;
-  obz = (R(3.0) * nz * mdn - q.mu[2]) * rr;
-}
-
-template <typename R>
-__device__ __forceinline__ R psr_shape(R rad, R rad0) { return R(0.5) * (R(1.0) - tanh((rad - rad0) / R(1.0))); }
-
-template <typename R>
-__device__ __forceinline__ bool psr_inside(const PsrBC<R>& q, const Phys& p, int i, int j, int k) {
-  const R ig = R(i + p.x0), jg = R(j + p.y0), kg = R(k + p.z0);
-  return ((ig - q.xc) * (ig - q.xc) + (jg - q.yc) * (jg - q.yc)) + (kg - q.zc) * (kg - q.zc) < q.sr2;
-}
-
-// New B (component comp) at a staggered point: user_psr.F90:157-214.
-template <typename R>
-__device__ __forceinline__ R psr_newB(const PsrBC<R>& q, R rx, R ry, R rz, R bint, R bown, int comp) {
-  const R rr_sqr = (rx * rx + ry * ry) + rz * rz;
-  R bdx, bdy, bdz;
-  psr_dipole(q, rx + q.xc, ry + q.yc, rz + q.zc, bdx, bdy, bdz);
-  const R bdip = (bdx * rx + bdy * ry) + bdz * rz;
-  const R rc = comp == 0 ? rx : (comp == 1 ? ry : rz);
-  const R bd = comp == 0 ? bdx : (comp == 1 ? bdy : bdz);
-  const R shift_B = R(4.0), scaleBperp = R(0.5), scaleBpar = R(0.25);
-  R sc = R(1.0) / scaleBperp;
-  R sh = psr_shape(sqrt(rr_sqr) * sc, (q.radius - shift_B) * sc);
-  const R v = (bint - bdip) * (rc / rr_sqr) * (R(1.0) - sh);
-  sc = R(1.0) / scaleBpar;
-  sh = psr_shape(sqrt(rr_sqr) * sc, (q.radius - shift_B) * sc);
-  return (v + bd) + ((bown - bint * rc / rr_sqr) - (bd - bdip * rc / rr_sqr)) * (R(1.0) - sh);
-}
-
-// New E (component comp) at a staggered point: user_psr.F90:219-297.
-template <typename R>
-__device__ __forceinline__ R psr_newE(const PsrBC<R>& q, R rx, R ry, R rz, R eint, R eown, int comp) {
-  const R rr_sqr = (rx * rx + ry * ry) + rz * rz;
-  R bdx, bdy, bdz;
-  psr_dipole(q, rx + q.xc, ry + q.yc, rz + q.zc, bdx, bdy, bdz);
-  const R vx = -(q.omega * ry), vy = q.omega * rx, vz = R(0.0);
-  const R exd = -(vy * bdz - vz * bdy) * q.ccinv;
-  const R eyd = (vx * bdz - vz * bdx) * q.ccinv;
-  const R ezd = -(vx * bdy - vy * bdx) * q.ccinv;
-  const R edip = (exd * rx + eyd * ry) + ezd * rz;
-  const R rc = comp == 0 ? rx : (comp == 1 ? ry : rz);
-  const R ed = comp == 0 ? exd : (comp == 1 ? eyd : ezd);
-  const R shift_E = R(0.0), scaleEpar = R(0.5), scaleEperp = R(0.25);
-  R sc = R(1.0) / scaleEpar;
-  R sh = psr_shape(sqrt(rr_sqr) * sc, (q.radius - shift_E) * sc);
-  const R v = ed + ((eown - eint * rc / rr_sqr) - (ed - edip * rc / rr_sqr)) * (R(1.0) - sh);
-  sc = R(1.0) / scaleEperp;
-  sh = psr_shape(sqrt(rr_sqr) * sc, (q.radius - shift_E) * sc);
-  return v + (eint - edip) * (rc / rr_sqr) * (R(1.0) - sh);
-}
-
 // Pass 1: new values of all six components for the cells of the bounding box
 // that lie inside r < 2R, written to a compact box buffer (6 * box cells).
 template <typename R>
@@ -228,44 +166,17 @@ __global__ void k_psr_bc(Geom g, Phys p, PsrBC<R> q, CEB<R> f, R* __restrict__ b
   if (bi >= q.bx || bj >= q.by) return;
   const int i = q.i_lo + bi, j = q.j_lo + bj, k = q.k_lo + bk;
   if (!psr_inside(q, p, i, j, k)) return;
-  const long long s = g.idx(i, j, k), dj = g.px, dk = g.plane;
-  const R *ex = f.c[0], *ey = f.c[1], *ez = f.c[2], *bx = f.c[3], *by = f.c[4], *bz = f.c[5];
-  const R ig = R(i + p.x0), jg = R(j + p.y0), kg = R(k + p.z0), h = R(0.5);
+  GAcc<R> a;
+  for (int c = 0; c < 6; ++c) a.f[c] = f.c[c];
+  a.s = g.idx(i, j, k);
+  a.dj = g.px;
+  a.dk = g.plane;
+  R o[6];
+  psr_cell(q, p, a, i, j, k, o);
   const long long nbox = (long long)q.bx * q.by * q.bz;
-  const long long o = bi + (long long)q.bx * (bj + (long long)q.by * bk);
-  R rx, ry, rz, in;
-  // B_x (:157-174)
-  rx = ig - q.xc; ry = (jg + h) - q.yc; rz = (kg + h) - q.zc;
-  in = (bx[s] * rx + R(0.25) * (((by[s] + by[s + dj]) + by[s - 1]) + by[s - 1 + dj]) * ry) +
-       R(0.25) * (((bz[s] + bz[s + dk]) + bz[s - 1]) + bz[s - 1 + dk]) * rz;
-  box[3 * nbox + o] = psr_newB(q, rx, ry, rz, in, bx[s], 0);
-  // B_y (:177-194)
-  rx = (ig + h) - q.xc; ry = jg - q.yc; rz = (kg + h) - q.zc;
-  in = (R(0.25) * (((bx[s] + bx[s + 1]) + bx[s - dj]) + bx[s + 1 - dj]) * rx + by[s] * ry) +
-       R(0.25) * (((bz[s] + bz[s + dk]) + bz[s - dj]) + bz[s - dj + dk]) * rz;
-  box[4 * nbox + o] = psr_newB(q, rx, ry, rz, in, by[s], 1);
-  // B_z (:197-214)
-  rx = (ig + h) - q.xc; ry = (jg + h) - q.yc; rz = kg - q.zc;
-  in = (R(0.25) * (((bx[s] + bx[s + 1]) + bx[s - dk]) + bx[s + 1 - dk]) * rx +
-        R(0.25) * (((by[s] + by[s + dj]) + by[s - dk]) + by[s + dj - dk]) * ry) +
-       bz[s] * rz;
-  box[5 * nbox + o] = psr_newB(q, rx, ry, rz, in, bz[s], 2);
-  // E_x (:219-243)
-  rx = (ig + h) - q.xc; ry = jg - q.yc; rz = kg - q.zc;
-  in = (ex[s] * rx + R(0.25) * (((ey[s] + ey[s + 1]) + ey[s - dj]) + ey[s + 1 - dj]) * ry) +
-       R(0.25) * (((ez[s] + ez[s + 1]) + ez[s - dk]) + ez[s + 1 - dk]) * rz;
-  box[0 * nbox + o] = psr_newE(q, rx, ry, rz, in, ex[s], 0);
-  // E_y (:246-270)
-  rx = ig - q.xc; ry = (jg + h) - q.yc; rz = kg - q.zc;
-  in = (R(0.25) * (((ex[s] + ex[s + dj]) + ex[s - 1]) + ex[s - 1 + dj]) * rx + ey[s] * ry) +
-       R(0.25) * (((ez[s] + ez[s + dj]) + ez[s - dk]) + ez[s + dj - dk]) * rz;
-  box[1 * nbox + o] = psr_newE(q, rx, ry, rz, in, ey[s], 1);
-  // E_z (:273-297)
-  rx = ig - q.xc; ry = jg - q.yc; rz = (kg + h) - q.zc;
-  in = (R(0.25) * (((ex[s] + ex[s + dk]) + ex[s - 1]) + ex[s - 1 + dk]) * rx +
-        R(0.25) * (((ey[s] + ey[s - dj]) + ey[s + dk]) + ey[s - dj + dk]) * ry) +
-       ez[s] * rz;
-  box[2 * nbox + o] = psr_newE(q, rx, ry, rz, in, ez[s], 2);
+  const long long ob = bi + (long long)q.bx * (bj + (long long)q.by * bk);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) box[c * nbox + ob] = o[c];
 }
 
 // Pass 2: copy the box values back for cells inside r < 2R (:305-325).
@@ -466,7 +377,7 @@ void launch_rho(const Geom& g, const R* ex, const R* ey, const R* ez, R* rho, cu
   k_rho<R><<<grid_for(g.sx + 3, g.sy + 3, g.sz + 3, B2), B2, 0, st>>>(g, ex, ey, ez, rho);
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 void launch_push(const Geom& g, R cc, const CEB<R>& eb, const CEB<R>& b0, bool has_b0, const R* rho, const EB<R>& d,
                  cudaStream_t st) {
   const dim3 gr = grid_for(g.sx, g.sy, g.sz, B2);
@@ -474,7 +385,7 @@ void launch_push(const Geom& g, R cc, const CEB<R>& eb, const CEB<R>& b0, bool h
   else k_push<R, C, false><<<gr, B2, 0, st>>>(g, cc, eb, b0, rho, d);
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2, R c3, bool incr, const EB<R>& f,
                    const CEB<R>& fn, const CEB<R>& df, cudaStream_t st) {
   const dim3 gr = grid_for(g.sx, g.sy, g.sz, B2);
@@ -482,7 +393,7 @@ void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2
   else k_update<R, C, false><<<gr, B2, 0, st>>>(g, p, ab, c1, c2, c3, incr, f, fn, df);
 }
 
-template <typename R, bool C>
+template <typename R, int C>
 void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStream_t st) {
   const dim3 gr = grid_for(g.sx, g.sy, g.sz, B2);
   CEB<R> c;
@@ -614,8 +525,9 @@ template int launch_waves<double>(const Geom&, const Phys&, const double[3], int
 
 FFE_INST_R(float)
 FFE_INST_R(double)
-FFE_INST_RC(float, false)
-FFE_INST_RC(float, true)
-FFE_INST_RC(double, false)
+FFE_INST_RC(float, 0)
+FFE_INST_RC(float, 1)
+FFE_INST_RC(float, 2)
+FFE_INST_RC(double, 0)
 
 }  // namespace ffe

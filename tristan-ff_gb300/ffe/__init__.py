@@ -32,7 +32,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "lib", "libffe_gb300.so")
 
 NG = 2
-FP64, FP32, FP32C = 0, 1, 2
+FP64, FP32, FP32C, FP32CD = 0, 1, 2, 3
 OPEN, PERIODIC, ABSORB = 0, 1, 2
 SETUP_NONE, SETUP_PSR, SETUP_UNIFORM, SETUP_LOOP = 0, 1, 2, 3
 PATH_AUTO, PATH_STAGED, PATH_FUSED, PATH_FUSED_EXACT = 0, 1, 2, 3
@@ -44,7 +44,7 @@ FIELDS = ("ex", "ey", "ez", "bx", "by", "bz", "b0x", "b0y", "b0z",
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ESTATE",
           -5: "ENONFINITE", -6: "ETIMEOUT", -7: "EUNSUPPORTED"}
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32c": FP32C}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32c": FP32C, "fp32cd": FP32CD}
 SETUPS = {"none": SETUP_NONE, "psr": SETUP_PSR, "uniform": SETUP_UNIFORM, "loop": SETUP_LOOP}
 
 # (ex, ey, ez, bx, by, bz) staggering offsets (user/user_psr.F90:54-63, 157-221)
