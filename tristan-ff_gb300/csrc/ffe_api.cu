@@ -145,6 +145,11 @@ template <typename R> Absorb<R> absorb_consts(ffe_t h) {
   return a;
 }
 
+// Launches of one ghost-plane pass of the user_uniform BC (below and above).
+int uniform_bc_launches(ffe_t h) {
+  return (h->p.z0 <= 1 ? 1 : 0) + (h->p.z0 + h->g.sz >= h->p.gsz ? 1 : 0);
+}
+
 // TINY added to the cleaning denominators only under FFE_FLAG_CLEAN_TINY.
 template <typename R> R clean_tiny(ffe_t h) {
   return (h->d.flags & FFE_FLAG_CLEAN_TINY) ? (sizeof(R) == 4 ? R(1e-7f) : R(1e-7)) : R(0);
@@ -250,7 +255,7 @@ int op_bc(ffe_t h, int step) {
       launch_psr_bc<R>(h->g, h->p, psr_consts<R>(h, step), eb_of<R>(h, h->cur), (R*)h->box, h->st);
       break;
     case FFE_SETUP_UNIFORM:
-      launch_uniform_bc<R>(h->g, h->p, uniform_consts<R>(h, step), eb_of<R>(h, h->cur), h->st);
+      launch_uniform_bc<R>(h->g, h->p, uniform_consts<R>(h, step), eb_of<R>(h, h->cur), false, h->st);
       break;
     case FFE_SETUP_LOOP:
       launch_loop_bc<R>(h->g, h->p, eb_of<R>(h, h->cur), h->st);
@@ -331,7 +336,8 @@ int step_staged(ffe_t h, int nsteps, int step0) {
 bool fused_possible(ffe_t h) {
   const int* b = h->d.boundary;
   const bool any_per = b[0] == 1 || b[1] == 1 || b[2] == 1;
-  return h->maps_ok && (h->d.setup == FFE_SETUP_NONE || (h->d.setup == FFE_SETUP_PSR && !any_per));
+  return h->maps_ok && (h->d.setup == FFE_SETUP_NONE || h->d.setup == FFE_SETUP_UNIFORM ||
+                        (h->d.setup == FFE_SETUP_PSR && !any_per));
 }
 
 template <typename R>
@@ -362,6 +368,7 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
   const Absorb<R> ab = absorb_consts<R>(h);
   const CEB<R> b0 = ceb_b0<R>(h);
   const bool psr = h->d.setup == FFE_SETUP_PSR;
+  const bool uni = h->d.setup == FFE_SETUP_UNIFORM;
   R* s1 = (R*)h->box;
   R* s2 = psr ? s1 + psr_fix_elems<R>(h) : nullptr;
   for (int n = 0; n < nsteps; ++n) {
@@ -369,6 +376,9 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
     const int ins[3] = {A, B, Cs}, outs[3] = {B, Cs, B};
     PsrBC<R> q{};
     if (psr) q = psr_consts<R>(h, step0 + n);
+    UniformBC<R> ub{};
+    if (uni) ub = uniform_consts<R>(h, step0 + n);
+    const UniformBC<R>* ubp = uni ? &ub : nullptr;
     for (int s = 0; s < 3; ++s) {
       double c[3];
       stage_coeffs<R>(s, c);
@@ -381,11 +391,11 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
       if (exact)
         lr = launch_fused_stage_exact<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi,
                                             me, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0,
-                                            eb_of<R>(h, outs[s]), ct, h->derr, h->st);
+                                            eb_of<R>(h, outs[s]), ct, ubp, h->derr, h->st);
       else
         lr = launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi, me,
                                       ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
-                                      ct, h->derr, h->st);
+                                      ct, ubp, h->derr, h->st);
       if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
       if ((rc = check_launch(h, "fused stage"))) return rc;
       if (psr) {
@@ -398,6 +408,10 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
                                  ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]), ct,
                                  s1, s2, h->st);
         if ((rc = check_launch(h, "pulsar boundary fix-up"))) return rc;
+      }
+      if (uni) {  // the ghost planes of the output set take this step's BC values
+        launch_uniform_bc<R>(h->g, h->p, ub, eb_of<R>(h, outs[s]), true, h->st);
+        if ((rc = check_launch(h, "uniform boundary ghosts"))) return rc;
       }
     }
     h->cur = B;
@@ -718,7 +732,7 @@ int ffe_step_launches(ffe_t h, int32_t* n) {
   if ((rc = ffe_step_path(h, &path))) return rc;
   if (path != FFE_PATH_STAGED) {
     // per stage: the fused kernel, plus the three box fix-up kernels of the pulsar BC
-    *n = h->d.setup == FFE_SETUP_PSR ? 12 : 3;
+    *n = h->d.setup == FFE_SETUP_PSR ? 12 : h->d.setup == FFE_SETUP_UNIFORM ? 3 + 3 * uniform_bc_launches(h) : 3;
     return FFE_OK;
   }
   // per stage: rho, push, update, [bc], [fill], clean + copy, [fill]

@@ -93,6 +93,8 @@ struct Params {
   const R* en_g[6];  // few halo cells computed at their periodic image (see below)
   R* out[6];
   int* err;
+  int ubc;            // apply the user_uniform BC inline (this step's constants in ub)
+  UniformBC<R> ub;
 };
 
 // Accessor over global arrays around linear index s (used for halo cells that
@@ -168,8 +170,10 @@ struct SmemNew {
   }
 };
 
+// One block's work: the TX x TY column (tile_x, tile_y) of a grid, planes of
+// z-chunk `chunk`.  Shared by the single-grid kernel and the batched kernel.
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
+__device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P, int tile_x, int tile_y, int chunk) {
   using S = Sizes<R>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R* old = reinterpret_cast<R*>(smem_raw);
@@ -178,8 +182,8 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(nw + S::NEW);
   const Geom g = P.g;
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int kb = blockIdx.z * P.kz;
+  const int x0 = tile_x * TX, y0 = tile_y * TY;
+  const int kb = chunk * P.kz;
   const int ke = min(kb + P.kz, g.sz);
   const bool per_x = P.p.bnd[0] == 1, per_y = P.p.bnd[1] == 1, per_z = P.p.bnd[2] == 1;
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
@@ -282,11 +286,12 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
     // block-uniform common case: every cell of the region is computed
     const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
                           !(mixed && (edge_xy || p <= 0 || p >= g.sz - 1));
-    bool push = true;
+    bool push = true, frozen_cell = false;
     if (!all_push) {
       const bool in_range = xy_in && p >= -1 && p <= g.sz;
       const bool out_z = p < 0 || p >= g.sz;
       const bool frozen = out_xy_open || (out_z && !per_z);
+      frozen_cell = in_range && frozen;
       if (!in_range || frozen) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) v[c] = in_range ? o1[c * S::OLDBOX] : R(0);
@@ -342,6 +347,18 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
         v[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
       if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, gi + P.p.y0, p + P.p.z0, v);
+    }
+    // Twisted-footpoint BC (user_uniform) between the update and the cleaning,
+    // on the planes z_glob <= 0 and >= gsz.  Frozen ghosts take the formula at
+    // their own position; a halo cell on a periodic face is the image of an
+    // interior cell, which took the formula at the image position.
+    if (P.ubc && (p + P.p.z0 <= 0 || p + P.p.z0 >= P.p.gsz)) {
+      int bi = gi, bj = gj;
+      if (!frozen_cell) {
+        bi = gi < 0 ? gi + g.sx : (gi >= g.sx ? gi - g.sx : gi);
+        bj = gj < 0 ? gj + g.sy : (gj >= g.sy ? gj - g.sy : gj);
+      }
+      uniform_bc_apply(P.ub, P.p, bi, bj, p, v[EX], v[EY], v[BZ]);
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c) dst[c * S::NEWPL] = v[c];
@@ -423,6 +440,25 @@ __global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps,
     }
     __syncthreads();
   }
+}
+
+// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
+__global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
+  stage_body<R, C, B0, ABS, STAGE1>(maps, P, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Many grids in one launch: block b takes work item b = (box, tile_x, tile_y,
+// z-chunk); each box's parameters and tensor maps sit in device tables.
+struct BatchItem {
+  int box, tx, ty, tz;
+};
+
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
+__global__ void __launch_bounds__(NT) k_fused_batch(const BatchItem* __restrict__ items, const Maps* __restrict__ maps,
+                                                    const Params<R>* __restrict__ params) {
+  const BatchItem it = items[blockIdx.x];
+  stage_body<R, C, B0, ABS, STAGE1>(maps[it.box], params[it.box], it.tx, it.ty, it.tz);
 }
 
 // ---- rotating-conductor boundary condition on the fused path ---------------
@@ -532,7 +568,7 @@ __global__ void k_fix_clean(const FixParams<R> F) {
   // cells of B+1 = U shrunk by one on every side, interior only
   const int bi = blockIdx.x * blockDim.x + threadIdx.x + 1, bj = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int bk = blockIdx.z + 1;
-  if (bi >= F.ux - 1 || bj >= F.uy - 1) return;
+  if (bi >= F.ux - 1 || bj >= F.uy - 1 || bk >= F.uz - 1) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   const Geom& g = F.g;
   if (i < 0 || i >= g.sx || j < 0 || j >= g.sy || k < 0 || k >= g.sz) return;
@@ -567,7 +603,8 @@ __global__ void k_fix_clean(const FixParams<R> F) {
 template <typename R, int C>
 int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
                     const void* maps_in, const void* maps_en, const CEB<R>& in_g, const CEB<R>& en_g,
-                    const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err, cudaStream_t st) {
+                    const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, const UniformBC<R>* ub, int* err,
+                    cudaStream_t st) {
   using namespace FFE_FUSED_NS;
   Maps M;
   memcpy(M.in, maps_in, sizeof(M.in));
@@ -589,6 +626,8 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
     P.en_g[c] = en_g.c[c];
   }
   P.err = err;
+  P.ubc = ub ? 1 : 0;
+  if (ub) P.ub = *ub;
   const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
   // enough blocks for ~16 per SM on 152 SMs, at least 8 planes per block
   const long long want = 152LL * 16;
@@ -719,7 +758,7 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
 #define FFE_INST_F(R, C)                                                                                        \
   template int FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,        \
                                      const void*, const void*, const CEB<R>&, const CEB<R>&, const CEB<R>&,     \
-                                     bool, const EB<R>&, R, int*, cudaStream_t);
+                                     bool, const EB<R>&, R, const UniformBC<R>*, int*, cudaStream_t);
 #define FFE_INST_X(R, C)                                                                                        \
   template int FFE_FIX_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, const PsrBC<R>&, R, R, R, R, bool, \
                                   int, const CEB<R>&, const CEB<R>&, const CEB<R>&, bool, const EB<R>&, R, R*,   \

@@ -22,7 +22,8 @@ void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], b
 template <typename R>
 void launch_psr_bc(const Geom& g, const Phys& p, const PsrBC<R>& q, const EB<R>& f, R* box, cudaStream_t st);
 template <typename R>
-void launch_uniform_bc(const Geom& g, const Phys& p, const UniformBC<R>& u, const EB<R>& f, cudaStream_t st);
+void launch_uniform_bc(const Geom& g, const Phys& p, const UniformBC<R>& u, const EB<R>& f, bool ghosts_only,
+                       cudaStream_t st);
 template <typename R>
 void launch_loop_bc(const Geom& g, const Phys& p, const EB<R>& f, cudaStream_t st);
 template <typename R>
@@ -48,17 +49,19 @@ void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
 // step-start set) made by make_stage_maps; err: device word set on a timeout.
 // Returns 0, or -3 if the kernel attribute could not be set.
 // ct: TINY added to the cleaning denominators (FFE_FLAG_CLEAN_TINY) or 0.
+// ub: the user_uniform BC constants of this step, applied inline (or null).
 // in_g / en_g: the same two sets as plain pointers (for halo cells computed at
 // their periodic image next to an open face).
 template <typename R, int C>
 int launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
                        int stage, const void* maps_in, const void* maps_en, const CEB<R>& in_g, const CEB<R>& en_g,
-                       const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err, cudaStream_t st);
+                       const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, const UniformBC<R>* ub, int* err,
+                       cudaStream_t st);
 template <typename R, int C>
 int launch_fused_stage_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
                              int stage, const void* maps_in, const void* maps_en, const CEB<R>& in_g,
-                             const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, int* err,
-                             cudaStream_t st);
+                             const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
+                             const UniformBC<R>* ub, int* err, cudaStream_t st);
 // Pulsar BC on the fused path: after a fused stage, redo the cells of the BC's
 // bounding box dilated by one (update on box+2 into s1, BC into s2, clean into
 // out).  s1, s2: 6 * (bx+4)(by+4)(bz+4) elements each.

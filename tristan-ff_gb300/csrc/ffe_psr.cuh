@@ -113,4 +113,37 @@ __device__ __forceinline__ void psr_cell(const PsrBC<R>& q, const Phys& p, const
   o[2] = psr_newE(q, rx, ry, rz, in, a(EZ, 0, 0, 0), 2);
 }
 
+// The twisted-footpoint BC of user/user_uniform.F90:114-142 at local cell
+// (i, j, k): on z_glob <= 0 it sets Ex, Ey to the rotating drive and Bz to the
+// tube profile, on z_glob >= gsz it resets Bz and zeroes Ex, Ey.  Pure
+// functions of position and time, so it applies to one cell at a time.
+template <typename R>
+__device__ __forceinline__ void uniform_bc_apply(const UniformBC<R>& u, const Phys& p, int i, int j, int k, R& ex,
+                                                 R& ey, R& bz) {
+  const R xg = R(i + p.x0), yg = R(j + p.y0), zg = R(k + p.z0), h = R(0.5);
+  R rx, ry, rr, omega, ee0;
+  if (zg <= R(0)) {
+    rx = (xg + h) - u.xc; ry = yg - u.yc;
+    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
+    omega = exp(-rr / u.r0) * u.beta * u.cc / u.r0;
+    ee0 = -omega * u.bnorm * u.tanh_t;
+    ex = rx * ee0;
+    rx = xg - u.xc; ry = (yg + h) - u.yc;
+    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
+    omega = exp(-rr / u.r0) * u.beta * u.cc / u.r0;
+    ee0 = -omega * u.bnorm * u.tanh_t;
+    ey = ry * ee0;
+    rx = (xg + h) - u.xc; ry = (yg + h) - u.yc;
+    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
+    bz = u.bnorm / (R(1.0) + (rr / u.r0));
+  }
+  if (zg >= R(p.gsz)) {
+    rx = (xg + h) - u.xc; ry = (yg + h) - u.yc;
+    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
+    bz = u.bnorm / (R(1.0) + (rr / u.r0));
+    ex = R(0.0);
+    ey = R(0.0);
+  }
+}
+
 }  // namespace ffe

@@ -203,31 +203,8 @@ __global__ void k_uniform_bc(Geom g, Phys p, UniformBC<R> u, EB<R> f, int k_firs
   const int j = blockIdx.y * blockDim.y + threadIdx.y - NG;
   const int k = k_first + (int)blockIdx.z;
   if (i >= g.sx + NG || j >= g.sy + NG || (int)blockIdx.z >= nk) return;
-  const R xg = R(i + p.x0), yg = R(j + p.y0), zg = R(k + p.z0), h = R(0.5);
   const long long s = g.idx(i, j, k);
-  R rx, ry, rr, omega, ee0;
-  if (zg <= R(0)) {
-    rx = (xg + h) - u.xc; ry = yg - u.yc;
-    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
-    omega = exp(-rr / u.r0) * u.beta * u.cc / u.r0;
-    ee0 = -omega * u.bnorm * u.tanh_t;
-    f.c[0][s] = rx * ee0;
-    rx = xg - u.xc; ry = (yg + h) - u.yc;
-    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
-    omega = exp(-rr / u.r0) * u.beta * u.cc / u.r0;
-    ee0 = -omega * u.bnorm * u.tanh_t;
-    f.c[1][s] = ry * ee0;
-    rx = (xg + h) - u.xc; ry = (yg + h) - u.yc;
-    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
-    f.c[5][s] = u.bnorm / (R(1.0) + (rr / u.r0));
-  }
-  if (zg >= R(p.gsz)) {
-    rx = (xg + h) - u.xc; ry = (yg + h) - u.yc;
-    rr = sqrt((rx * rx + ry * ry) + tiny<R>());
-    f.c[5][s] = u.bnorm / (R(1.0) + (rr / u.r0));
-    f.c[0][s] = R(0.0);
-    f.c[1][s] = R(0.0);
-  }
+  uniform_bc_apply(u, p, i, j, k, f.c[0][s], f.c[1][s], f.c[5][s]);
 }
 
 // ---- user_loop boundary condition (user/user_loop.F90:115-163) ------------
@@ -425,11 +402,17 @@ void launch_psr_bc(const Geom& g, const Phys& p, const PsrBC<R>& q, const EB<R>&
 }
 
 template <typename R>
-void launch_uniform_bc(const Geom& g, const Phys& p, const UniformBC<R>& u, const EB<R>& f, cudaStream_t st) {
-  // planes k with k + z0 <= 0 or k + z0 >= gsz, k in [-2, sz+1]
+void launch_uniform_bc(const Geom& g, const Phys& p, const UniformBC<R>& u, const EB<R>& f, bool ghosts_only,
+                       cudaStream_t st) {
+  // planes k with k + z0 <= 0 or k + z0 >= gsz, k in [-2, sz+1]; the fused
+  // path applies the BC to the interior plane itself and asks for ghosts only
   const int klo = -NG, khi = g.sz + NG - 1;
   int a_hi = std::min(khi, -p.z0);              // z_glob <= 0
   int b_lo = std::max(klo, p.gsz - p.z0);       // z_glob >= gsz
+  if (ghosts_only) {
+    a_hi = std::min(a_hi, -1);
+    b_lo = std::max(b_lo, g.sz);
+  }
   const dim3 b(32, 8, 1);
   if (a_hi >= klo) {
     const int nk = a_hi - klo + 1;
@@ -509,7 +492,8 @@ template int launch_waves<double>(const Geom&, const Phys&, const double[3], int
   template void launch_rho<R>(const Geom&, const R*, const R*, const R*, R*, cudaStream_t);                      \
   template void launch_fill<R>(const Geom&, const Phys&, const EB<R>&, R* const[3], bool, cudaStream_t);         \
   template void launch_psr_bc<R>(const Geom&, const Phys&, const PsrBC<R>&, const EB<R>&, R*, cudaStream_t);     \
-  template void launch_uniform_bc<R>(const Geom&, const Phys&, const UniformBC<R>&, const EB<R>&, cudaStream_t); \
+  template void launch_uniform_bc<R>(const Geom&, const Phys&, const UniformBC<R>&, const EB<R>&, bool,          \
+                                     cudaStream_t);                                                             \
   template void launch_loop_bc<R>(const Geom&, const Phys&, const EB<R>&, cudaStream_t);                         \
   template void launch_psr_init<R>(const Geom&, const Phys&, const PsrBC<R>&, const EB<R>&, cudaStream_t);       \
   template void launch_uniform_init<R>(const Geom&, const Phys&, const UniformBC<R>&, R*, R*, cudaStream_t);     \
