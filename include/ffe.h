@@ -226,6 +226,42 @@ int ffe_synchronize(ffe_t h);
 /* Wait for the handle's stream, giving up after timeout_ms (FFE_ETIMEOUT). */
 int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms);
 
+/* --- batches: many meshblocks advanced together ------------------------- */
+/* No counterpart in the reference (one meshblock per MPI rank there).  A batch
+   groups handles created by ffe_create on the current device, all with the
+   same precision (FFE_FP64, FFE_FP32 or FFE_FP32C) and all able to take the
+   fused path (path AUTO or FUSED; setup none, uniform, or psr with no
+   periodic axis).  The batch does not own the handles; destroy it first.
+   Each SSP-RK3 stage of all members is one kernel launch over the tiles of
+   every member (plus one batched launch per stage for user_uniform ghost
+   planes and three for the pulsar fix-up); the launches of a call are
+   captured into a CUDA graph and replayed.  Members keep their own set
+   rotation and step counter: results equal those of ffe_step on each member
+   with the same tiling.  stream: a cudaStream_t or NULL (own stream).     */
+typedef struct ffe_batch ffe_batch;
+typedef ffe_batch* ffe_batch_t;
+int ffe_batch_create(ffe_batch_t* out, const ffe_t* members, int32_t n, void* stream);
+int ffe_batch_destroy(ffe_batch_t b);
+/* Advance every member nsteps steps; member m's first step is step0[m]
+   (step0 NULL: 0 for all).  Orders itself after the work queued on each
+   member's stream and makes those streams wait for it.  Asynchronous. */
+int ffe_batch_step(ffe_batch_t b, int32_t nsteps, const int32_t* step0);
+/* Tiling of the batched stage kernel: tile height (8 or 16; 16 needs FP32 or
+   FP32C), z-planes per block (0 = per-member default), persistent blocks
+   (1: one resident wave of blocks takes the work items in turn). */
+int ffe_batch_set_tiling(ffe_batch_t b, int32_t tile_y, int32_t planes, int32_t persistent);
+int ffe_batch_get_tiling(ffe_batch_t b, int32_t* tile_y, int32_t* planes, int32_t* persistent);
+/* Time every tiling candidate on the members' current fields (a stage launch
+   that writes only the set the next step overwrites; member state is
+   unchanged), keep the fastest and return its time per stage in *best_ms.
+   reps: timed launches per candidate (>= 1). */
+int ffe_batch_autotune(ffe_batch_t b, int32_t reps, double* best_ms);
+/* Kernel launches per step (nodes of the captured graph per step). */
+int ffe_batch_launches(ffe_batch_t b, int32_t* per_step);
+/* Wait for the batch's stream; FFE_ETIMEOUT if a stage block gave up waiting
+   for its copies. */
+int ffe_batch_synchronize(ffe_batch_t b);
+
 int ffe_abi_version(void);
 
 #ifdef __cplusplus

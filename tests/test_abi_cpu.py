@@ -59,3 +59,15 @@ def test_create_rejects_bad_descriptors_without_a_gpu(lib):
     buf = ctypes.create_string_buffer(256)
     assert L.ffe_last_error(None, buf, 256) == -1
     assert b"ghost zones" in buf.value
+
+
+def test_batch_entry_points_validate_arguments_without_a_gpu(lib):
+    L = ffe.load_library()
+    b = ctypes.c_void_p()
+    assert L.ffe_batch_create(ctypes.byref(b), None, 0, None) == -1
+    assert L.ffe_batch_step(None, 1, None) == -1
+    assert L.ffe_batch_set_tiling(None, 8, 0, 0) == -1
+    assert L.ffe_batch_autotune(None, 1, None) == -1
+    n = ctypes.c_int32()
+    assert L.ffe_batch_launches(None, ctypes.byref(n)) == -1
+    assert L.ffe_batch_destroy(None) == 0

@@ -7,6 +7,7 @@ Translation units (compiled in parallel, then linked):
   csrc/ffe_staged.cu   one kernel per reference procedure, -fmad=false
   csrc/ffe_fused.cu    fused stage kernels (fast: contraction on)
   csrc/ffe_fused.cu    again with -DFFE_FUSED_EXACT -fmad=false (verification path)
+  csrc/ffe_fused.cu    with -DFFE_BATCH_TY=8 and =16: batched (many-grid) launches
 Output: tristan-ff_gb300/lib/libffe_gb300.so (git-ignored; rebuilt on each box).
 """
 import os
@@ -29,6 +30,8 @@ UNITS = [
     ("ffe_staged.cu", "ffe_staged.o", ["-fmad=false"]),
     ("ffe_fused.cu", "ffe_fused_fast.o", []),
     ("ffe_fused.cu", "ffe_fused_exact.o", ["-fmad=false", "-DFFE_FUSED_EXACT"]),
+    ("ffe_fused.cu", "ffe_batch_t8.o", ["-DFFE_BATCH_TY=8"]),
+    ("ffe_fused.cu", "ffe_batch_t16.o", ["-DFFE_BATCH_TY=16"]),
     ("ffe_noalloc.cu", "ffe_noalloc.o", ["-fmad=false"]),
 ]
 

@@ -22,6 +22,8 @@
 #include <thread>
 #include <string>
 #include <new>
+#include <vector>
+#include <algorithm>
 #include <cuda.h>
 #include "../../include/ffe.h"
 #include "ffe_kernels.h"
@@ -575,7 +577,7 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   h->maps_ok = true;
   for (int s = 0; s < 3 && h->maps_ok; ++s)
     for (int c = 0; c < 6 && h->maps_ok; ++c)
-      h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es) == 0;
+      h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es, 8) == 0;
   if (!h->maps_ok && d.path >= FFE_PATH_FUSED) {
     cudaFree(h->arena);
     if (h->own_stream) cudaStreamDestroy(h->st);
@@ -808,6 +810,645 @@ int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms) {
     if (ms >= timeout_ms) return fail(h, FFE_ETIMEOUT, "stream not idle after %d ms", timeout_ms);
     std::this_thread::sleep_for(std::chrono::microseconds(200));
   }
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches (ffe_batch_*): many meshblocks advanced together.
+//
+// Members are split into groups of up to BATCH_MAX.  Each SSP-RK3 stage of a
+// group is ONE k_fused_batch launch over the work items (member, tile,
+// z-chunk) of all its members; every member has an entry (BatchBox) in the
+// launch's parameter table with its stage constants, its set pointers (the
+// member's own set rotation) and this step's boundary constants.  Pulsar
+// members add one batched fix-up (three launches) per stage, user_uniform
+// members one batched ghost-plane launch.  The launches of a chunk of up to
+// kChunk steps are captured into a CUDA graph; a later chunk of the same
+// length updates the instantiated graph in place (same topology, new
+// parameters) and replays it.
+// ===========================================================================
+
+struct ffe_batch {
+  struct Group {
+    int first = 0, n = 0;          // members [first, first + n)
+    BatchItem* ditems = nullptr;   // stage work items (box = index in the group)
+    int nitems = 0, cap = 0;
+    FixItem* dghost = nullptr;     // user_uniform ghost-plane items (box = index in the group)
+    int nghost = 0;
+  };
+  struct G {
+    int steps;
+    cudaGraphExec_t exec;
+  };
+  int device = 0;
+  int precision = FFE_FP32;
+  std::vector<ffe_t> m;
+  std::vector<Group> groups;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev = nullptr;      // ordering with member streams
+  cudaEvent_t copied = nullptr;  // host staging of the fix-up table free again
+  int ty = 8, kz = 0, persistent = 0;
+  int blocks_per_sm = 0, sms = 0;
+  int* derr = nullptr;           // device timeout word
+  CUtensorMap* dmaps = nullptr;  // device: [tile 8|16][member][set][12 maps]
+  std::vector<int> kz_of;        // planes per block of each member
+  FixItem* dfix = nullptr;       // pulsar fix-up items (box = pulsar index)
+  int nfix = 0;
+  std::vector<int> psr;          // members with the pulsar fix-up
+  std::vector<unsigned char> tabs;  // host: BoxTable per (step, stage, group) of a chunk
+  void* dfixtab = nullptr;       // device: FixParams [steps][3][pulsar members]
+  void* hfixtab = nullptr;       // pinned staging of the fix-up table
+  int fix_steps = 0;             // capacity of the fix-up tables in steps
+  std::vector<G> graphs;         // instantiated graphs, by chunk length
+};
+
+namespace {
+
+constexpr int kChunk = 256;  // steps per captured graph
+
+int bfail(int st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  t_status = st;
+  return st;
+}
+
+#define BCUDA(call)                                                                          \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return bfail(FFE_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t fix_entry_bytes(int prec) {
+  return prec == FFE_FP64 ? sizeof(FixParams<double>) : sizeof(FixParams<float>);
+}
+
+void drop_graphs(ffe_batch* b) {
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  b->graphs.clear();
+}
+
+int tile_index(int ty) { return ty == 16 ? 1 : 0; }
+
+// Work items of the current tiling per group, largest blocks first (the
+// hardware and the persistent loop both take items in order).
+int build_items(ffe_batch* b) {
+  const int nm = (int)b->m.size();
+  b->kz_of.assign(nm, 0);
+  for (auto& gr : b->groups) {
+    std::vector<std::pair<long long, BatchItem>> it;
+    for (int l = 0; l < gr.n; ++l) {
+      const int i = gr.first + l;
+      const Geom& g = b->m[i]->g;
+      const int kz = b->kz ? std::min(b->kz, g.sz) : fused_planes_per_block(g, b->ty);
+      b->kz_of[i] = kz;
+      const int tx = (g.sx + FUSED_TX - 1) / FUSED_TX, tyn = (g.sy + b->ty - 1) / b->ty, tz = (g.sz + kz - 1) / kz;
+      for (int z = 0; z < tz; ++z)
+        for (int y = 0; y < tyn; ++y)
+          for (int x = 0; x < tx; ++x) {
+            const long long w = (long long)std::min(FUSED_TX, g.sx - x * FUSED_TX) *
+                                std::min(b->ty, g.sy - y * b->ty) * std::min(kz, g.sz - z * kz);
+            it.push_back({w, BatchItem{l, x, y, z}});
+          }
+    }
+    std::stable_sort(it.begin(), it.end(), [](const auto& a, const auto& c) { return a.first > c.first; });
+    std::vector<BatchItem> v(it.size());
+    for (size_t k = 0; k < it.size(); ++k) v[k] = it[k].second;
+    if ((int)v.size() > gr.cap) {
+      if (gr.ditems) cudaFree(gr.ditems);
+      gr.ditems = nullptr;
+      gr.cap = 0;
+      BCUDA(cudaMalloc(&gr.ditems, v.size() * sizeof(BatchItem)));
+      gr.cap = (int)v.size();
+    }
+    gr.nitems = (int)v.size();
+    if (!v.empty())
+      BCUDA(cudaMemcpyAsync(gr.ditems, v.data(), v.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, b->st));
+  }
+  BCUDA(cudaStreamSynchronize(b->st));
+  return FFE_OK;
+}
+
+// Tile height 16 exists for FP32 storage only (its rings do not fit in FP64).
+template <typename R, int C> int prepare_kernels(int ty) {
+  if constexpr (sizeof(R) == 4)
+    if (ty == 16) return fused_batch_prepare_t16<R, C>();
+  return fused_batch_prepare_t8<R, C>();
+}
+template <typename R, int C>
+int launch_batch_kernel(const ffe_batch* b, const ffe_batch::Group& gr, bool stage1, const BoxTable<R>& T,
+                        int grid) {
+  if constexpr (sizeof(R) == 4)
+    if (b->ty == 16) return launch_fused_batch_t16<R, C>(stage1, gr.ditems, gr.nitems, T, grid, b->st);
+  return launch_fused_batch_t8<R, C>(stage1, gr.ditems, gr.nitems, T, grid, b->st);
+}
+
+int prepare(ffe_batch* b) {
+  int n = 0;
+  if (b->precision == FFE_FP64) n = b->ty == 8 ? prepare_kernels<double, 0>(8) : 0;
+  else if (b->precision == FFE_FP32C) n = prepare_kernels<float, 1>(b->ty);
+  else n = prepare_kernels<float, 0>(b->ty);
+  if (n <= 0) return bfail(FFE_ECUDA, "batched stage kernel: cannot raise the shared-memory limit");
+  b->blocks_per_sm = n;
+  return FFE_OK;
+}
+
+int launch_grid(const ffe_batch* b, const ffe_batch::Group& gr) {
+  if (!b->persistent) return gr.nitems;
+  return std::max(1, std::min(gr.nitems, b->blocks_per_sm * b->sms));
+}
+
+template <typename R> BoxTable<R>* host_table(ffe_batch* b, int n, int s, int gi) {
+  const size_t k = ((size_t)n * 3 + s) * b->groups.size() + gi;
+  return reinterpret_cast<BoxTable<R>*>(b->tabs.data()) + k;
+}
+
+// Fill the launch tables for steps [n0, n0 + cn) of this call.
+template <typename R, int C>
+void fill_tables(ffe_batch* b, const std::vector<int>& cur0, const int32_t* step0, int n0, int cn) {
+  const int np = (int)b->psr.size(), nm = (int)b->m.size();
+  b->tabs.assign((size_t)cn * 3 * b->groups.size() * sizeof(BoxTable<R>), 0);
+  FixParams<R>* ftab = (FixParams<R>*)b->hfixtab;
+  const int ti = tile_index(b->ty);
+  for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
+    const auto& gr = b->groups[gi];
+    for (int l = 0; l < gr.n; ++l) {
+      const int i = gr.first + l;
+      ffe_t h = b->m[i];
+      const Absorb<R> ab = absorb_consts<R>(h);
+      const R ct = clean_tiny<R>(h);
+      const bool uni = h->d.setup == FFE_SETUP_UNIFORM;
+      const int pi = (int)(std::find(b->psr.begin(), b->psr.end(), i) - b->psr.begin());
+      for (int n = 0; n < cn; ++n) {
+        const int ts = (step0 ? step0[i] : 0) + n0 + n;
+        const int A = (cur0[i] + n0 + n) % 3, B = (A + 1) % 3, Cs = (A + 2) % 3;
+        const int ins[3] = {A, B, Cs}, outs[3] = {B, Cs, B};
+        UniformBC<R> ub{};
+        if (uni) ub = uniform_consts<R>(h, ts);
+        PsrBC<R> q{};
+        if (pi < np) q = psr_consts<R>(h, ts);
+        for (int s = 0; s < 3; ++s) {
+          double c[3];
+          stage_coeffs<R>(s, c);
+          const bool incr = C && std::fabs(c[0] + c[1] - 1.0) < 1e-6;
+          BatchBox<R>& e = host_table<R>(b, n, s, gi)->b[l];
+          Params<R>& P = e.P;
+          P.g = h->g;
+          P.p = h->p;
+          P.ab = ab;
+          P.cc = R(h->d.cc);
+          P.c1 = R(c[0]);
+          P.c2 = R(c[1]);
+          P.c3 = R(c[2]);
+          P.ct = ct;
+          P.incr = incr ? 1 : 0;
+          P.kz = b->kz_of[i];
+          for (int k = 0; k < 3; ++k) P.b0[k] = (const R*)h->b0[k];
+          for (int k = 0; k < 6; ++k) {
+            P.in_g[k] = (const R*)h->set[ins[s]][k];
+            P.en_g[k] = (const R*)h->set[A][k];
+            P.out[k] = (R*)h->set[outs[s]][k];
+          }
+          P.err = b->derr;
+          P.ubc = uni ? 1 : 0;
+          P.ub = ub;
+          e.mi = b->dmaps + (((size_t)ti * nm + i) * 3 + ins[s]) * 12;
+          e.me = b->dmaps + (((size_t)ti * nm + i) * 3 + A) * 12 + 6;
+          e.has_b0 = h->has_b0 ? 1 : 0;
+          e.absorb = h->p.bnd[0] == 2 ? 1 : 0;
+          if (pi < np) {
+            FixParams<R>& F = ftab[((size_t)n * 3 + s) * np + pi];
+            memset(&F, 0, sizeof F);
+            F.g = h->g;
+            F.p = h->p;
+            F.ab = ab;
+            F.q = q;
+            F.cc = P.cc;
+            F.c1 = P.c1;
+            F.c2 = P.c2;
+            F.c3 = P.c3;
+            F.ct = ct;
+            F.incr = P.incr;
+            int u[6];
+            psr_fix_box(h->g, q.i_lo, q.i_hi, q.j_lo, q.j_hi, q.k_lo, q.k_hi, u);
+            F.ui = u[0]; F.uj = u[1]; F.uk = u[2]; F.ux = u[3]; F.uy = u[4]; F.uz = u[5];
+            for (int k = 0; k < 6; ++k) {
+              F.in[k] = P.in_g[k];
+              F.en[k] = P.en_g[k];
+              F.out[k] = P.out[k];
+            }
+            for (int k = 0; k < 3; ++k) F.b0[k] = P.b0[k];
+            F.s1 = (R*)h->box;
+            F.s2 = (R*)h->box + psr_fix_elems<R>(h);
+            F.has_b0 = e.has_b0;
+            F.absorb = e.absorb;
+          }
+        }
+      }
+    }
+  }
+}
+
+// All launches of stage s of step n of the current chunk.
+template <typename R, int C>
+int launch_stage(ffe_batch* b, int n, int s) {
+  const int np = (int)b->psr.size();
+  for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
+    const auto& gr = b->groups[gi];
+    const BoxTable<R>& T = *host_table<R>(b, n, s, gi);
+    if (launch_batch_kernel<R, C>(b, gr, s == 0, T, launch_grid(b, gr))) return bfail(FFE_ECUDA, "batched stage launch");
+    if (gr.nghost) launch_uniform_ghosts_batch<R>(gr.dghost, gr.nghost, T, b->st);
+  }
+  if (b->nfix)
+    launch_fix_batch<R, C>(s == 0, b->dfix, b->nfix,
+                           (const FixParams<R>*)b->dfixtab + ((size_t)n * 3 + s) * np, b->st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return bfail(FFE_ECUDA, "batched launch: %s", cudaGetErrorString(e));
+  return FFE_OK;
+}
+
+// Capture the cn steps of the filled tables; instantiate, or update the
+// cached graph of the same length in place.
+template <typename R, int C>
+int capture(ffe_batch* b, int cn, cudaGraphExec_t* out) {
+  BCUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int rc = FFE_OK;
+  for (int n = 0; n < cn && rc == FFE_OK; ++n)
+    for (int s = 0; s < 3 && rc == FFE_OK; ++s) rc = launch_stage<R, C>(b, n, s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return bfail(FFE_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+  for (auto& c : b->graphs)
+    if (c.steps == cn) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(c.exec, g, &info) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        *out = c.exec;
+        return FFE_OK;
+      }
+      cudaGetLastError();
+      cudaGraphExecDestroy(c.exec);
+      c = b->graphs.back();
+      b->graphs.pop_back();
+      break;
+    }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bfail(FFE_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  b->graphs.push_back({cn, *out});
+  return FFE_OK;
+}
+
+int ensure_fix_tables(ffe_batch* b, int steps) {
+  const int np = (int)b->psr.size();
+  if (!np || steps <= b->fix_steps) return FFE_OK;
+  const size_t fb = (size_t)steps * 3 * np * fix_entry_bytes(b->precision);
+  BCUDA(cudaStreamSynchronize(b->st));
+  drop_graphs(b);
+  if (b->dfixtab) cudaFree(b->dfixtab);
+  if (b->hfixtab) cudaFreeHost(b->hfixtab);
+  b->dfixtab = b->hfixtab = nullptr;
+  b->fix_steps = 0;
+  BCUDA(cudaMalloc(&b->dfixtab, fb));
+  BCUDA(cudaMallocHost(&b->hfixtab, fb));
+  b->fix_steps = steps;
+  return FFE_OK;
+}
+
+// Order the batch stream after each member's queued work; returns the
+// members' current sets.
+template <typename R>
+int join_members(ffe_batch* b, std::vector<int>& cur0) {
+  int rc;
+  const int nm = (int)b->m.size();
+  cur0.resize(nm);
+  for (int i = 0; i < nm; ++i) {
+    ffe_t h = b->m[i];
+    if ((rc = sync_ghosts<R>(h))) return rc;
+    BCUDA(cudaEventRecord(b->ev, h->st));
+    BCUDA(cudaStreamWaitEvent(b->st, b->ev, 0));
+    cur0[i] = h->cur;
+  }
+  return FFE_OK;
+}
+
+template <typename R, int C>
+int batch_run(ffe_batch* b, int nsteps, const int32_t* step0) {
+  int rc;
+  std::vector<int> cur0;
+  if ((rc = join_members<R>(b, cur0))) return rc;
+  if ((rc = ensure_fix_tables(b, std::min(nsteps, kChunk)))) return rc;
+  const int np = (int)b->psr.size();
+  for (int n0 = 0; n0 < nsteps; n0 += kChunk) {
+    const int cn = std::min(kChunk, nsteps - n0);
+    BCUDA(cudaEventSynchronize(b->copied));  // the previous chunk's fix-up table has left the staging buffer
+    fill_tables<R, C>(b, cur0, step0, n0, cn);
+    if (np) {
+      BCUDA(cudaMemcpyAsync(b->dfixtab, b->hfixtab, (size_t)cn * 3 * np * sizeof(FixParams<R>),
+                            cudaMemcpyHostToDevice, b->st));
+      BCUDA(cudaEventRecord(b->copied, b->st));
+    }
+    cudaGraphExec_t ex = nullptr;
+    if ((rc = capture<R, C>(b, cn, &ex))) return rc;
+    BCUDA(cudaGraphLaunch(ex, b->st));
+  }
+  BCUDA(cudaEventRecord(b->ev, b->st));
+  for (int i = 0; i < (int)b->m.size(); ++i) {
+    ffe_t h = b->m[i];
+    h->cur = (cur0[i] + nsteps) % 3;
+    BCUDA(cudaStreamWaitEvent(h->st, b->ev, 0));
+  }
+  return FFE_OK;
+}
+
+// Time the stage launches of all groups for the current tiling, in the form
+// of stage 2 with the stage input equal to the step start (both the current
+// set); the output is the set that stage 2 of the next step overwrites.
+template <typename R, int C>
+int time_stage(ffe_batch* b, int reps, double* ms) {
+  int rc;
+  std::vector<int> cur0;
+  if ((rc = join_members<R>(b, cur0))) return rc;
+  if ((rc = ensure_fix_tables(b, 1))) return rc;
+  BCUDA(cudaEventSynchronize(b->copied));
+  fill_tables<R, C>(b, cur0, nullptr, 0, 1);
+  for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
+    BoxTable<R>* T = host_table<R>(b, 0, 1, gi);
+    for (int l = 0; l < b->groups[gi].n; ++l) {
+      BatchBox<R>& e = T->b[l];
+      const int A = cur0[b->groups[gi].first + l];
+      for (int k = 0; k < 6; ++k) e.P.in_g[k] = (const R*)b->m[b->groups[gi].first + l]->set[A][k];
+      e.mi = e.me - 6;
+    }
+  }
+  cudaEvent_t t0, t1;
+  BCUDA(cudaEventCreate(&t0));
+  BCUDA(cudaEventCreate(&t1));
+  float best = 1e30f;
+  bool bad = false;
+  for (int r = -1; r < reps && !bad; ++r) {  // r = -1: warm-up
+    cudaEventRecord(t0, b->st);
+    for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
+      const auto& gr = b->groups[gi];
+      bad |= launch_batch_kernel<R, C>(b, gr, false, *host_table<R>(b, 0, 1, gi), launch_grid(b, gr)) != 0;
+    }
+    cudaEventRecord(t1, b->st);
+    bad |= cudaEventSynchronize(t1) != cudaSuccess || cudaGetLastError() != cudaSuccess;
+    float t = 0;
+    cudaEventElapsedTime(&t, t0, t1);
+    if (r >= 0) best = std::min(best, t);
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (bad) return bfail(FFE_ECUDA, "autotune launch failed");
+  *ms = best;
+  int err = 0;
+  BCUDA(cudaMemcpy(&err, b->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return bfail(FFE_ETIMEOUT, "a batched stage block timed out waiting for its plane copies");
+  return FFE_OK;
+}
+
+#define BDISPATCH(b, FN, ...)                                \
+  ((b)->precision == FFE_FP64    ? FN<double, 0>(__VA_ARGS__) \
+   : (b)->precision == FFE_FP32C ? FN<float, 1>(__VA_ARGS__)  \
+                                 : FN<float, 0>(__VA_ARGS__))
+
+int set_tiling(ffe_batch* b, int ty, int kz, int persistent) {
+  if (ty != 8 && ty != 16) return bfail(FFE_EINVAL, "tile height must be 8 or 16");
+  if (ty == 16 && b->precision == FFE_FP64) return bfail(FFE_EUNSUPPORTED, "tile height 16 needs FP32 storage");
+  if (kz < 0) return bfail(FFE_EINVAL, "planes per block must be >= 0");
+  BCUDA(cudaStreamSynchronize(b->st));
+  drop_graphs(b);
+  b->ty = ty;
+  b->kz = kz;
+  b->persistent = persistent ? 1 : 0;
+  int rc;
+  if ((rc = prepare(b))) return rc;
+  return build_items(b);
+}
+
+void free_batch(ffe_batch* b) {
+  if (b->st) cudaStreamSynchronize(b->st);
+  drop_graphs(b);
+  for (auto& gr : b->groups) {
+    if (gr.ditems) cudaFree(gr.ditems);
+    if (gr.dghost) cudaFree(gr.dghost);
+  }
+  if (b->dfix) cudaFree(b->dfix);
+  if (b->dfixtab) cudaFree(b->dfixtab);
+  if (b->hfixtab) cudaFreeHost(b->hfixtab);
+  if (b->dmaps) cudaFree(b->dmaps);
+  if (b->derr) cudaFree(b->derr);
+  if (b->ev) cudaEventDestroy(b->ev);
+  if (b->copied) cudaEventDestroy(b->copied);
+  if (b->own_stream && b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+int check_batch(ffe_batch_t b) {
+  if (!b) return bfail(FFE_EINVAL, "null batch");
+  BCUDA(cudaSetDevice(b->device));
+  return FFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffe_batch_create(ffe_batch_t* out, const ffe_t* members, int32_t n, void* stream) {
+  if (!out || !members || n <= 0) return bfail(FFE_EINVAL, "ffe_batch_create: need n > 0 members");
+  *out = nullptr;
+  int dev = 0;
+  BCUDA(cudaGetDevice(&dev));
+  const int prec = members[0] ? members[0]->d.precision : -1;
+  for (int i = 0; i < n; ++i) {
+    ffe_t h = members[i];
+    if (!h) return bfail(FFE_EINVAL, "member %d is null", i);
+    for (int j = 0; j < i; ++j)
+      if (members[j] == h) return bfail(FFE_EINVAL, "member %d appears twice", i);
+    if (h->device != dev) return bfail(FFE_EINVAL, "member %d lives on device %d, not %d", i, h->device, dev);
+    if (h->d.precision != prec) return bfail(FFE_EINVAL, "members must share one precision");
+    if (prec == FFE_FP32CD) return bfail(FFE_EUNSUPPORTED, "batches run FP64, FP32 or FP32C");
+    if (h->d.path == FFE_PATH_STAGED || h->d.path == FFE_PATH_FUSED_EXACT || !fused_possible(h))
+      return bfail(FFE_EUNSUPPORTED, "member %d cannot take the fused path (setup %d, path %d)", i, h->d.setup,
+                   h->d.path);
+  }
+  ffe_batch* b = new (std::nothrow) ffe_batch();
+  if (!b) return bfail(FFE_ENOMEM, "host allocation failed");
+  b->device = dev;
+  b->precision = prec;
+  b->m.assign(members, members + n);
+  for (int f = 0; f < n; f += BATCH_MAX) {
+    ffe_batch::Group gr;
+    gr.first = f;
+    gr.n = std::min(BATCH_MAX, n - f);
+    b->groups.push_back(gr);
+  }
+  int rc = FFE_OK;
+  auto cu = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == FFE_OK) rc = bfail(FFE_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    return rc == FFE_OK;
+  };
+  if (stream) {
+    b->st = (cudaStream_t)stream;
+  } else if (cu(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking), "cudaStreamCreate")) {
+    b->own_stream = true;
+  }
+  cudaDeviceProp prop;
+  if (rc == FFE_OK && cu(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties"))
+    b->sms = prop.multiProcessorCount;
+  if (rc == FFE_OK) cu(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming), "cudaEventCreate");
+  if (rc == FFE_OK) cu(cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming), "cudaEventCreate");
+  if (rc == FFE_OK && cu(cudaMalloc(&b->derr, 256), "cudaMalloc")) cu(cudaMemset(b->derr, 0, 256), "cudaMemset");
+  // tensor maps of every member's sets for both tile heights
+  if (rc == FFE_OK) {
+    std::vector<CUtensorMap> maps((size_t)2 * n * 3 * 12);
+    for (int t = 0; t < 2 && rc == FFE_OK; ++t)
+      for (int i = 0; i < n && rc == FFE_OK; ++i)
+        for (int s = 0; s < 3 && rc == FFE_OK; ++s)
+          for (int c = 0; c < 6 && rc == FFE_OK; ++c) {
+            CUtensorMap* e = &maps[(((size_t)t * n + i) * 3 + s) * 12];
+            ffe_t h = members[i];
+            if (make_stage_maps(&e[c], &e[6 + c], h->set[s][c], h->g, (int)h->es, t ? 16 : 8))
+              rc = bfail(FFE_EUNSUPPORTED, "cannot encode TMA tensor maps for member %d", i);
+          }
+    if (rc == FFE_OK && cu(cudaMalloc(&b->dmaps, maps.size() * sizeof(CUtensorMap)), "cudaMalloc"))
+      cu(cudaMemcpy(b->dmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "cudaMemcpy");
+  }
+  // pulsar fix-up items (all members) and user_uniform ghost-plane items (per group)
+  if (rc == FFE_OK) {
+    std::vector<FixItem> fx;
+    for (auto& gr : b->groups) {
+      std::vector<FixItem> gh;
+      for (int l = 0; l < gr.n; ++l) {
+        ffe_t h = members[gr.first + l];
+        if (h->d.setup == FFE_SETUP_PSR) {
+          const PsrBC<float> q = psr_consts<float>(h, 0);  // the box does not depend on the step
+          if (q.bx > 0 && q.by > 0 && q.bz > 0) {
+            const int pi = (int)b->psr.size();
+            b->psr.push_back(gr.first + l);
+            int u[6];
+            psr_fix_box(h->g, q.i_lo, q.i_hi, q.j_lo, q.j_hi, q.k_lo, q.k_hi, u);
+            for (int z = 0; z < u[5]; ++z)
+              for (int y = 0; y < (u[4] + 7) / 8; ++y)
+                for (int x = 0; x < (u[3] + 31) / 32; ++x) fx.push_back(FixItem{pi, x, y, z});
+          }
+        }
+        if (h->d.setup == FFE_SETUP_UNIFORM) {
+          // ghost planes with z_glob <= 0 or >= gsz (interior planes take the BC inside the stage kernel)
+          const int sz = h->g.sz, z0 = h->p.z0, gsz = h->p.gsz;
+          for (int k = -NG; k < sz + NG; ++k) {
+            if (k >= 0 && k < sz) continue;
+            if (!(k + z0 <= 0 || k + z0 >= gsz)) continue;
+            for (int y = 0; y < (h->g.sy + 2 * NG + 7) / 8; ++y)
+              for (int x = 0; x < (h->g.sx + 2 * NG + 31) / 32; ++x) gh.push_back(FixItem{l, x, y, k});
+          }
+        }
+      }
+      gr.nghost = (int)gh.size();
+      if (rc == FFE_OK && !gh.empty() && cu(cudaMalloc(&gr.dghost, gh.size() * sizeof(FixItem)), "cudaMalloc"))
+        cu(cudaMemcpy(gr.dghost, gh.data(), gh.size() * sizeof(FixItem), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    b->nfix = (int)fx.size();
+    if (rc == FFE_OK && !fx.empty() && cu(cudaMalloc(&b->dfix, fx.size() * sizeof(FixItem)), "cudaMalloc"))
+      cu(cudaMemcpy(b->dfix, fx.data(), fx.size() * sizeof(FixItem), cudaMemcpyHostToDevice), "cudaMemcpy");
+  }
+  if (rc == FFE_OK) cu(cudaEventRecord(b->copied, b->st), "cudaEventRecord");
+  if (rc == FFE_OK) rc = set_tiling(b, 8, 0, 0);
+  if (rc != FFE_OK) {
+    free_batch(b);
+    return rc;
+  }
+  *out = b;
+  return FFE_OK;
+}
+
+int ffe_batch_destroy(ffe_batch_t b) {
+  if (!b) return FFE_OK;
+  cudaSetDevice(b->device);
+  free_batch(b);
+  return FFE_OK;
+}
+
+int ffe_batch_step(ffe_batch_t b, int32_t nsteps, const int32_t* step0) {
+  int rc;
+  if ((rc = check_batch(b))) return rc;
+  if (nsteps < 0) return bfail(FFE_EINVAL, "nsteps < 0");
+  if (nsteps == 0) return FFE_OK;
+  return BDISPATCH(b, batch_run, b, nsteps, step0);
+}
+
+int ffe_batch_set_tiling(ffe_batch_t b, int32_t tile_y, int32_t planes, int32_t persistent) {
+  int rc;
+  if ((rc = check_batch(b))) return rc;
+  return set_tiling(b, tile_y, planes, persistent);
+}
+
+int ffe_batch_get_tiling(ffe_batch_t b, int32_t* tile_y, int32_t* planes, int32_t* persistent) {
+  if (!b || !tile_y || !planes || !persistent) return bfail(FFE_EINVAL, "null argument");
+  *tile_y = b->ty;
+  *planes = b->kz;
+  *persistent = b->persistent;
+  return FFE_OK;
+}
+
+int ffe_batch_autotune(ffe_batch_t b, int32_t reps, double* best_ms) {
+  int rc;
+  if ((rc = check_batch(b))) return rc;
+  if (reps < 1) return bfail(FFE_EINVAL, "reps must be >= 1");
+  const int tys[2] = {8, 16}, kzs[5] = {0, 8, 16, 32, 64};
+  double best = 1e300;
+  int bt = 8, bk = 0, bp = 0;
+  for (int t : tys) {
+    if (t == 16 && b->precision == FFE_FP64) continue;
+    for (int k : kzs)
+      for (int p = 0; p < 2; ++p) {
+        if ((rc = set_tiling(b, t, k, p))) return rc;
+        double ms = 0;
+        if ((rc = BDISPATCH(b, time_stage, b, reps, &ms))) return rc;
+        if (ms < best) {
+          best = ms;
+          bt = t;
+          bk = k;
+          bp = p;
+        }
+      }
+  }
+  if ((rc = set_tiling(b, bt, bk, bp))) return rc;
+  if (best_ms) *best_ms = best;
+  return FFE_OK;
+}
+
+int ffe_batch_launches(ffe_batch_t b, int32_t* per_step) {
+  if (!b || !per_step) return bfail(FFE_EINVAL, "null argument");
+  int ng = 0;
+  for (auto& gr : b->groups) ng += gr.nghost ? 1 : 0;
+  *per_step = 3 * ((int)b->groups.size() + ng + (b->nfix ? 3 : 0));
+  return FFE_OK;
+}
+
+int ffe_batch_synchronize(ffe_batch_t b) {
+  int rc;
+  if ((rc = check_batch(b))) return rc;
+  BCUDA(cudaStreamSynchronize(b->st));
+  int e = 0;
+  BCUDA(cudaMemcpyAsync(&e, b->derr, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  BCUDA(cudaStreamSynchronize(b->st));
+  if (e) {
+    BCUDA(cudaMemsetAsync(b->derr, 0, sizeof(int), b->st));
+    return bfail(FFE_ETIMEOUT, "a batched stage block timed out waiting for its plane copies");
+  }
+  return FFE_OK;
 }
 
 }  // extern "C"

@@ -35,15 +35,22 @@
 // Compiled twice: normally (multiply-add contraction and, in FP32, the
 // reciprocal-multiply quotient) as the fast path, and with -fmad=false under
 // FFE_FUSED_EXACT with correctly rounded division (bit-comparable with the
-// oracle).
+// oracle).  Compiled a third and fourth time with -DFFE_BATCH_TY=8 / 16 for the
+// batched launches (many grids per launch, see k_fused_batch).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cstring>
 #include "ffe_kernels.h"
+#include "ffe_fused_types.cuh"
 #include "ffe_physics.cuh"
 #include "ffe_psr.cuh"
 
-#ifdef FFE_FUSED_EXACT
+#if defined(FFE_BATCH_TY)
+#define FFE_CAT2(a, b) a##b
+#define FFE_CAT(a, b) FFE_CAT2(a, b)
+#define FFE_FUSED_NS FFE_CAT(fused_batch, FFE_BATCH_TY)
+#define FFE_FAST true
+#elif defined(FFE_FUSED_EXACT)
 #define FFE_FUSED_NS fused_exact
 #define FFE_FAST false
 #else
@@ -54,47 +61,30 @@
 namespace ffe {
 namespace FFE_FUSED_NS {
 
-constexpr int TX = 32, TY = 8;
+constexpr int TX = FUSED_TX;
 constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+TX+1)
-constexpr int OH = TY + 4;               // OLD box rows (y0-2 .. y0+TY+1)
-constexpr int EH = TY + 2;               // EN box rows (y0-1 .. y0+TY)
-constexpr int NX = TX + 2, NY = TY + 2;  // NEW tile (tile + 1 halo)
-constexpr int NCELL = NX * NY;           // 340
-constexpr int NT = (NCELL + 31) / 32 * 32;  // 352 threads: one per NEW cell
+constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
 constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
-template <typename R> struct Sizes {
-  static constexpr int OLDBOX = ((OW * OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);  // elements
-  static constexpr int ENBOX = ((OW * EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
-  static constexpr int NEWPL = NY * NX;  // one component of one NEW plane
+// Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
+// rows (y0-1 .. y0+TY), NEW planes of NY rows, one thread per NEW cell
+// (TY = 8: 34 x 10 = 340 cells, 352 threads).
+template <int TY>
+struct Tile {
+  static constexpr int OH = TY + 4, EH = TY + 2, NY = TY + 2;
+  static constexpr int NCELL = NX * NY;
+  static constexpr int NT = (NCELL + 31) / 32 * 32;
+};
+
+template <typename R, int TY> struct Sizes {
+  static constexpr int OLDBOX = ((OW * Tile<TY>::OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
+  static constexpr int ENBOX = ((OW * Tile<TY>::EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
+  static constexpr int NEWPL = Tile<TY>::NY * NX;  // one component of one NEW plane
   static constexpr int OLD = DO * 6 * OLDBOX;
   static constexpr int EN = DE * 6 * ENBOX;
   static constexpr int NEW = DN * 6 * NEWPL;
   static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * (DO + DE);
-};
-
-struct Maps {  // one 3-D tensor map per component: stage input (OLD) and step start (EN)
-  CUtensorMap in[6];
-  CUtensorMap en[6];
-};
-
-template <typename R>
-struct Params {
-  Geom g;
-  Phys p;
-  Absorb<R> ab;
-  R cc, c1, c2, c3;
-  R ct;  // TINY in the cleaning denominator (opt-in), else 0
-  int incr;
-  int kz;  // planes per block
-  const R* b0[3];
-  const R* in_g[6];  // stage input and step-start sets in global memory, for the
-  const R* en_g[6];  // few halo cells computed at their periodic image (see below)
-  R* out[6];
-  int* err;
-  int ubc;            // apply the user_uniform BC inline (this step's constants in ub)
-  UniformBC<R> ub;
 };
 
 // Accessor over global arrays around linear index s (used for halo cells that
@@ -117,6 +107,9 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
 }
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(unsigned bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -149,32 +142,36 @@ __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map
 
 // Accessor over the OLD ring for push_cell: b[dk+1] points at this thread's
 // cell in plane p+dk, so every (component, di, dj) offset is a constant.
-template <typename R>
+template <typename R, int TY>
 struct SmemOld {
   const R* b[3];
   const R* const* b0;
   long long gs, dj, dk;  // global index of the cell (for B0)
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
     if (c >= 6) return __ldg(b0[c - 6] + gs + di + djj * dj + dkk * dk);
-    return b[dkk + 1][c * Sizes<R>::OLDBOX + djj * OW + di];
+    return b[dkk + 1][c * Sizes<R, TY>::OLDBOX + djj * OW + di];
   }
   __device__ __forceinline__ R rho(int di, int djj, int dkk) const { return rho_at<R>(*this, di, djj, dkk); }
 };
 
 // Accessor over the NEW ring for clean_cell.
-template <typename R>
+template <typename R, int TY>
 struct SmemNew {
   const R* b[3];
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
-    return b[dkk + 1][c * Sizes<R>::NEWPL + djj * NX + di];
+    return b[dkk + 1][c * Sizes<R, TY>::NEWPL + djj * NX + di];
   }
 };
 
 // One block's work: the TX x TY column (tile_x, tile_y) of a grid, planes of
 // z-chunk `chunk`.  Shared by the single-grid kernel and the batched kernel.
-template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P, int tile_x, int tile_y, int chunk) {
-  using S = Sizes<R>;
+// mi / me: the six tensor maps of the stage-input and step-start sets.
+// Returns false when a wait on a copy gave up (the error word is set).
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY>
+__device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensorMap* me, const Params<R>& P,
+                                           int tile_x, int tile_y, int chunk) {
+  using S = Sizes<R, TY>;
+  constexpr int OH = Tile<TY>::OH, EH = Tile<TY>::EH, NCELL = Tile<TY>::NCELL;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R* old = reinterpret_cast<R*>(smem_raw);
   R* en = old + S::OLD;
@@ -205,7 +202,7 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
     mbar_expect_tx(bar, 6u * OW * OH * sizeof(R));
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), &maps.in[c], x0, y0, p + NG, bar);
+      tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), mi + c, x0, y0, p + NG, bar);
   };
   auto issue_en = [&](int p) {
     const int s = (p - kb + 1) % DE;
@@ -213,7 +210,7 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
     mbar_expect_tx(bar, 6u * OW * EH * sizeof(R));
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), &maps.en[c], x0, y0 + 1, p + NG, bar);
+      tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), me + c, x0, y0 + 1, p + NG, bar);
   };
   if (tid == 0) {
     for (int s = 0; s < DO + DE; ++s) mbar_init(smem_u32(bars + s), 1);
@@ -328,7 +325,7 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
       }
     }
     if (push) {
-      SmemOld<R> a;
+      SmemOld<R, TY> a;
       a.b[0] = oth + so * (6 * S::OLDBOX);
       a.b[1] = o1;
       a.b[2] = oth + s2 * (6 * S::OLDBOX);
@@ -338,7 +335,7 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
       a.dk = g.plane;
       R d[6];
       if constexpr (FD) push_cell_fast<B0>(a, cc, d);
-      else push_cell<R, C, B0, SmemOld<R>, false>(a, cc, d);
+      else push_cell<R, C, B0, SmemOld<R, TY>, false>(a, cc, d);
       const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
@@ -381,13 +378,13 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
   // clean plane k (m = k - kb: NEW slots of k-1, k, k+1 are m, m+1, m+2 mod 4)
   auto clean_store = [&](int k, int m) {
     if (!c_in) return;
-    SmemNew<R> a;
+    SmemNew<R, TY> a;
     a.b[0] = cth + (m & (DN - 1)) * (6 * S::NEWPL);
     a.b[1] = cth + ((m + 1) & (DN - 1)) * (6 * S::NEWPL);
     a.b[2] = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
     R e[3];
     if constexpr (FD) clean_cell_fast(a, e, ct);
-    else clean_cell<R, C, SmemNew<R>, false>(a, e, ct);
+    else clean_cell<R, C, SmemNew<R, TY>, false>(a, e, ct);
     const R v[6] = {e[0], e[1], e[2], a(BX, 0, 0, 0), a(BY, 0, 0, 0), a(BZ, 0, 0, 0)};
     const bool z_image = per_z && (k < NG || k >= g.sz - NG);
     if ((no_xy_images || !xy_images) && !z_image) {
@@ -439,27 +436,49 @@ __device__ __forceinline__ void stage_body(const Maps& maps, const Params<R>& P,
           mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1));
     }
     __syncthreads();
+    return false;
+  }
+  // Every wait of this chunk has completed: invalidate the barriers so that a
+  // persistent block may initialise them again for its next work item.
+  __syncthreads();
+  if (tid == 0)
+    for (int s = 0; s < DO + DE; ++s) mbar_inval(smem_u32(bars + s));
+  return true;
+}
+
+#if !defined(FFE_BATCH_TY)
+// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).  Tile height 8.
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
+__global__ void __launch_bounds__(Tile<8>::NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
+  stage_body<R, C, B0, ABS, STAGE1, 8>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+#else
+// Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
+// the grids' parameters and tensor-map pointers come in the kernel's
+// parameter space (a table of up to BATCH_MAX entries), so that, as in
+// k_fused, every per-grid constant is read from the constant bank where it is
+// used instead of occupying registers.  The B0 / absorbing-layer variant is
+// chosen per grid.  With fewer blocks than items the blocks are persistent:
+// block b takes items b, b + gridDim.x, ... (the host orders items by
+// decreasing work).
+template <typename R, int C, bool STAGE1, int TY>
+__global__ void __launch_bounds__(Tile<TY>::NT, (sizeof(R) == 4 && TY == 8) ? 2 : 1)
+    k_fused_batch(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const BatchItem it = items[w];
+    const BatchBox<R>& e = T.b[it.box];
+    bool ok;
+    if (e.has_b0) {
+      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, true, false, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+    } else {
+      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, false, false, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+    }
+    if (!ok) return;
   }
 }
-
-// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
-  stage_body<R, C, B0, ABS, STAGE1>(maps, P, blockIdx.x, blockIdx.y, blockIdx.z);
-}
-
-// Many grids in one launch: block b takes work item b = (box, tile_x, tile_y,
-// z-chunk); each box's parameters and tensor maps sit in device tables.
-struct BatchItem {
-  int box, tx, ty, tz;
-};
-
-template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(NT) k_fused_batch(const BatchItem* __restrict__ items, const Maps* __restrict__ maps,
-                                                    const Params<R>* __restrict__ params) {
-  const BatchItem it = items[blockIdx.x];
-  stage_body<R, C, B0, ABS, STAGE1>(maps[it.box], params[it.box], it.tx, it.ty, it.tz);
-}
+#endif
 
 // ---- rotating-conductor boundary condition on the fused path ---------------
 // The fused kernel cleans every cell before any boundary condition could act.
@@ -472,22 +491,8 @@ __global__ void __launch_bounds__(NT) k_fused_batch(const BatchItem* __restrict_
 //   k_fix_clean:  clean the interior cells of B+1 from S2, store E'' and B'
 // S1, S2 are compact U-shaped arrays (6 components).  Only for grids with no
 // periodic axis (the pulsar runs open or absorbing), so U holds no image.
-template <typename R>
-struct FixParams {
-  Geom g;
-  Phys p;
-  Absorb<R> ab;
-  PsrBC<R> q;
-  R cc, c1, c2, c3, ct;
-  int incr;
-  int ui, uj, uk, ux, uy, uz;  // U: first cell and extents
-  const R* in[6];
-  const R* en[6];
-  const R* b0[3];
-  R* out[6];
-  R* s1;
-  R* s2;
-};
+// Each step is a per-cell function of U coordinates (bi, bj, bk), launched
+// over one grid (k_fix_*) or over many grids at once (k_fix_*_batch).
 
 template <typename R>
 struct BoxAcc {  // accessor over a compact U array around a cell
@@ -499,11 +504,9 @@ struct BoxAcc {  // accessor over a compact U array around a cell
 };
 
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void k_fix_update(const FixParams<R> F) {
+__device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, int bj, int bk) {
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
-  const int bi = blockIdx.x * blockDim.x + threadIdx.x, bj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int bk = blockIdx.z;
-  if (bi >= F.ux || bj >= F.uy) return;
+  if (bi >= F.ux || bj >= F.uy || bk >= F.uz) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   const Geom& g = F.g;
   const long long n = (long long)F.ux * F.uy * F.uz;
@@ -536,10 +539,8 @@ __global__ void k_fix_update(const FixParams<R> F) {
 }
 
 template <typename R>
-__global__ void k_fix_bc(const FixParams<R> F) {
-  const int bi = blockIdx.x * blockDim.x + threadIdx.x, bj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int bk = blockIdx.z;
-  if (bi >= F.ux || bj >= F.uy) return;
+__device__ __forceinline__ void fix_bc_cell(const FixParams<R>& F, int bi, int bj, int bk) {
+  if (bi >= F.ux || bj >= F.uy || bk >= F.uz) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   const long long n = (long long)F.ux * F.uy * F.uz;
   const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
@@ -562,12 +563,13 @@ __global__ void k_fix_bc(const FixParams<R> F) {
   }
 }
 
+// (bi, bj, bk): U coordinates less one (the cells of B+1 start at U + 1).
 template <typename R, int C>
-__global__ void k_fix_clean(const FixParams<R> F) {
+__device__ __forceinline__ void fix_clean_cell(const FixParams<R>& F, int bi, int bj, int bk) {
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
-  // cells of B+1 = U shrunk by one on every side, interior only
-  const int bi = blockIdx.x * blockDim.x + threadIdx.x + 1, bj = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int bk = blockIdx.z + 1;
+  ++bi;
+  ++bj;
+  ++bk;
   if (bi >= F.ux - 1 || bj >= F.uy - 1 || bk >= F.uz - 1) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   const Geom& g = F.g;
@@ -592,8 +594,66 @@ __global__ void k_fix_clean(const FixParams<R> F) {
   F.out[5][s] = a(BZ, 0, 0, 0);
 }
 
+#if !defined(FFE_BATCH_TY)
+// One grid: block (x, y) covers 32 x 8 cells of a U plane, blockIdx.z the plane.
+template <typename R, int C, bool B0, bool ABS, bool STAGE1>
+__global__ void k_fix_update(const FixParams<R> F) {
+  fix_update_cell<R, C, B0, ABS, STAGE1>(F, blockIdx.x * blockDim.x + threadIdx.x,
+                                         blockIdx.y * blockDim.y + threadIdx.y, blockIdx.z);
+}
+template <typename R>
+__global__ void k_fix_bc(const FixParams<R> F) {
+  fix_bc_cell<R>(F, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.z);
+}
+template <typename R, int C>
+__global__ void k_fix_clean(const FixParams<R> F) {
+  fix_clean_cell<R, C>(F, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
+                       blockIdx.z);
+}
+#elif FFE_BATCH_TY == 8
+// Many grids: block b takes item b = (grid, 32-wide x block, 8-high y block,
+// plane) of that grid's U box; a 32 x 8 thread block.
+template <typename R, int C, bool STAGE1>
+__global__ void k_fix_update_batch(const FixItem* __restrict__ items, const FixParams<R>* __restrict__ fp) {
+  const FixItem it = items[blockIdx.x];
+  const FixParams<R>& F = fp[it.box];
+  const int bi = it.bx * 32 + threadIdx.x, bj = it.by * 8 + threadIdx.y;
+  if (F.has_b0) {
+    if (F.absorb) fix_update_cell<R, C, true, true, STAGE1>(F, bi, bj, it.bz);
+    else fix_update_cell<R, C, true, false, STAGE1>(F, bi, bj, it.bz);
+  } else {
+    if (F.absorb) fix_update_cell<R, C, false, true, STAGE1>(F, bi, bj, it.bz);
+    else fix_update_cell<R, C, false, false, STAGE1>(F, bi, bj, it.bz);
+  }
+}
+template <typename R>
+__global__ void k_fix_bc_batch(const FixItem* __restrict__ items, const FixParams<R>* __restrict__ fp) {
+  const FixItem it = items[blockIdx.x];
+  fix_bc_cell<R>(fp[it.box], it.bx * 32 + threadIdx.x, it.by * 8 + threadIdx.y, it.bz);
+}
+template <typename R, int C>
+__global__ void k_fix_clean_batch(const FixItem* __restrict__ items, const FixParams<R>* __restrict__ fp) {
+  const FixItem it = items[blockIdx.x];
+  fix_clean_cell<R, C>(fp[it.box], it.bx * 32 + threadIdx.x, it.by * 8 + threadIdx.y, it.bz);
+}
+
+// user_uniform ghost planes of many grids: item = (grid, x block, y block,
+// plane k); the grid's output set, geometry and this step's constants come
+// from its stage-launch entry.
+template <typename R>
+__global__ void k_uniform_ghosts_batch(const FixItem* __restrict__ items, const __grid_constant__ BoxTable<R> T) {
+  const FixItem it = items[blockIdx.x];
+  const Params<R>& P = T.b[it.box].P;
+  const int i = it.bx * 32 + (int)threadIdx.x - NG, j = it.by * 8 + (int)threadIdx.y - NG;
+  if (i >= P.g.sx + NG || j >= P.g.sy + NG) return;
+  const long long s = P.g.idx(i, j, it.bz);
+  uniform_bc_apply(P.ub, P.p, i, j, it.bz, P.out[0][s], P.out[1][s], P.out[5][s]);
+}
+#endif
+
 }  // namespace FFE_FUSED_NS
 
+#if !defined(FFE_BATCH_TY)
 #ifdef FFE_FUSED_EXACT
 #define FFE_LAUNCH_NAME launch_fused_stage_exact
 #else
@@ -628,14 +688,12 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.err = err;
   P.ubc = ub ? 1 : 0;
   if (ub) P.ub = *ub;
+  constexpr int TY = 8;
   const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
-  // enough blocks for ~16 per SM on 152 SMs, at least 8 planes per block
-  const long long want = 152LL * 16;
-  int kz = (int)std::max(8LL, std::min<long long>(64, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
-  kz = std::min(kz, g.sz);
+  const int kz = fused_planes_per_block(g, TY);
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
-  const size_t smem = Sizes<R>::BYTES;
+  const size_t smem = Sizes<R, TY>::BYTES;
   const bool abs = p.bnd[0] == 2;
   const bool s1 = stage == 1;
 #define FFE_GO(B0V, ABSV, S1V)                                                                   \
@@ -648,7 +706,7 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
         return -3;                                                                               \
       attr_set = true;                                                                           \
     }                                                                                            \
-    kf<<<grid, NT, smem, st>>>(M, P);                                                            \
+    kf<<<grid, Tile<TY>::NT, smem, st>>>(M, P);                                                  \
   } while (0)
   if (has_b0) {
     if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
@@ -666,16 +724,6 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
 #else
 #define FFE_FIX_NAME launch_psr_fixup
 #endif
-
-// U = the pulsar BC's bounding box dilated by two cells, clipped to the array.
-static void psr_fix_box(const Geom& g, int i_lo, int i_hi, int j_lo, int j_hi, int k_lo, int k_hi, int u[6]) {
-  u[0] = std::max(-NG, i_lo - 2);
-  u[1] = std::max(-NG, j_lo - 2);
-  u[2] = std::max(-NG, k_lo - 2);
-  u[3] = std::min(g.sx + NG - 1, i_hi + 2) - u[0] + 1;
-  u[4] = std::min(g.sy + NG - 1, j_hi + 2) - u[1] + 1;
-  u[5] = std::min(g.sz + NG - 1, k_hi + 2) - u[2] + 1;
-}
 
 template <typename R, int C>
 int FFE_FIX_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<R>& q, R cc, R c1, R c2, R c3,
@@ -705,6 +753,8 @@ int FFE_FIX_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<
   for (int c = 0; c < 3; ++c) F.b0[c] = b0.c[c];
   F.s1 = s1;
   F.s2 = s2;
+  F.has_b0 = has_b0 ? 1 : 0;
+  F.absorb = p.bnd[0] == 2 ? 1 : 0;
   const dim3 b(32, 8, 1), gr((F.ux + 31) / 32, (F.uy + 7) / 8, F.uz);
   const bool abs = p.bnd[0] == 2, s1st = stage == 1;
 #define FFE_FIXGO(B0V, ABSV, S1V) k_fix_update<R, C, B0V, ABSV, S1V><<<gr, b, 0, st>>>(F)
@@ -724,12 +774,22 @@ int FFE_FIX_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<
 #ifndef FFE_FUSED_EXACT
 void fused_tile_shape(int* tx, int* ty) {
   *tx = fused_fast::TX;
-  *ty = fused_fast::TY;
+  *ty = 8;
 }
 
-// Tensor maps of one array for the fused kernels: the OLD box (tile + 2 halo)
-// and the EN box (tile + 1 halo rows).  Coordinates: (i + 2, j + 2, k + 2).
-int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es) {
+// z-planes per block: enough blocks for ~16 per SM on 152 SMs, at least 8
+// planes per block, at most 64.
+int fused_planes_per_block(const Geom& g, int ty) {
+  const int tiles_x = (g.sx + FUSED_TX - 1) / FUSED_TX, tiles_y = (g.sy + ty - 1) / ty;
+  const long long want = 152LL * 16;
+  const int kz = (int)std::max(8LL, std::min<long long>(64, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
+  return std::min(kz, g.sz);
+}
+
+// Tensor maps of one array for the fused kernels of tile height ty: the OLD
+// box (tile + 2 halo) and the EN box (tile + 1 halo rows).  Coordinates:
+// (i + 2, j + 2, k + 2).
+int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es, int ty) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -744,8 +804,8 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
   const cuuint64_t strides[2] = {(cuuint64_t)g.px * es, (cuuint64_t)g.plane * es};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  const cuuint32_t box_old[3] = {(cuuint32_t)OW, (cuuint32_t)OH, 1};
-  const cuuint32_t box_en[3] = {(cuuint32_t)OW, (cuuint32_t)EH, 1};
+  const cuuint32_t box_old[3] = {(cuuint32_t)OW, (cuuint32_t)(ty + 4), 1};
+  const cuuint32_t box_en[3] = {(cuuint32_t)OW, (cuuint32_t)(ty + 2), 1};
   CUresult r = encode((CUtensorMap*)map_old, dt, 3, base, dims, strides, box_old, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return -2;
@@ -771,5 +831,79 @@ FFE_INST_X(float, 0)
 FFE_INST_X(float, 1)
 FFE_INST_X(float, 2)
 FFE_INST_X(double, 0)
+
+#else  // FFE_BATCH_TY: batched launches for tile height FFE_BATCH_TY
+
+#define FFE_BATCH_LAUNCH FFE_CAT(launch_fused_batch_t, FFE_BATCH_TY)
+#define FFE_BATCH_PREP FFE_CAT(fused_batch_prepare_t, FFE_BATCH_TY)
+
+// One stage of many grids: `grid` blocks over nitems work items.  The
+// shared-memory limit must have been raised by FFE_BATCH_PREP (this launch
+// may be captured into a graph, where that call does not belong).
+template <typename R, int C>
+int FFE_BATCH_LAUNCH(bool stage1, const BatchItem* items, int nitems, const BoxTable<R>& T, int grid,
+                     cudaStream_t st) {
+  using namespace FFE_FUSED_NS;
+  constexpr int TY = FFE_BATCH_TY;
+  const size_t smem = Sizes<R, TY>::BYTES;
+  if (nitems <= 0) return 0;
+  if (stage1) k_fused_batch<R, C, true, TY><<<grid, Tile<TY>::NT, smem, st>>>(items, nitems, T);
+  else k_fused_batch<R, C, false, TY><<<grid, Tile<TY>::NT, smem, st>>>(items, nitems, T);
+  return 0;
+}
+
+// Raise the shared-memory limit of both batched stage kernels; returns their
+// resident blocks per SM, or 0 on failure.
+template <typename R, int C>
+int FFE_BATCH_PREP() {
+  using namespace FFE_FUSED_NS;
+  constexpr int TY = FFE_BATCH_TY;
+  const size_t smem = Sizes<R, TY>::BYTES;
+  auto k1 = k_fused_batch<R, C, true, TY>;
+  auto k2 = k_fused_batch<R, C, false, TY>;
+  if (cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  if (cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  int n1 = 0, n2 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k1, Tile<TY>::NT, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k2, Tile<TY>::NT, smem) != cudaSuccess) return 0;
+  return n1 < n2 ? n1 : n2;
+}
+
+#define FFE_INST_B(R, C)                                                                                 \
+  template int FFE_BATCH_LAUNCH<R, C>(bool, const BatchItem*, int, const BoxTable<R>&, int, cudaStream_t); \
+  template int FFE_BATCH_PREP<R, C>();
+FFE_INST_B(float, 0)
+FFE_INST_B(float, 1)
+#if FFE_BATCH_TY == 8
+FFE_INST_B(double, 0)
+
+// Pulsar fix-up of many grids: the three steps, each one launch over all items.
+template <typename R, int C>
+int launch_fix_batch(bool stage1, const FixItem* items, int nitems, const FixParams<R>* fp, cudaStream_t st) {
+  using namespace FFE_FUSED_NS;
+  if (nitems <= 0) return 0;
+  const dim3 b(32, 8, 1);
+  if (stage1) k_fix_update_batch<R, C, true><<<nitems, b, 0, st>>>(items, fp);
+  else k_fix_update_batch<R, C, false><<<nitems, b, 0, st>>>(items, fp);
+  k_fix_bc_batch<R><<<nitems, b, 0, st>>>(items, fp);
+  k_fix_clean_batch<R, C><<<nitems, b, 0, st>>>(items, fp);
+  return 0;
+}
+
+template <typename R>
+int launch_uniform_ghosts_batch(const FixItem* items, int nitems, const BoxTable<R>& T, cudaStream_t st) {
+  using namespace FFE_FUSED_NS;
+  if (nitems <= 0) return 0;
+  k_uniform_ghosts_batch<R><<<nitems, dim3(32, 8, 1), 0, st>>>(items, T);
+  return 0;
+}
+
+template int launch_fix_batch<float, 0>(bool, const FixItem*, int, const FixParams<float>*, cudaStream_t);
+template int launch_fix_batch<float, 1>(bool, const FixItem*, int, const FixParams<float>*, cudaStream_t);
+template int launch_fix_batch<double, 0>(bool, const FixItem*, int, const FixParams<double>*, cudaStream_t);
+template int launch_uniform_ghosts_batch<float>(const FixItem*, int, const BoxTable<float>&, cudaStream_t);
+template int launch_uniform_ghosts_batch<double>(const FixItem*, int, const BoxTable<double>&, cudaStream_t);
+#endif
+#endif  // FFE_BATCH_TY
 
 }  // namespace ffe

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cuda_runtime.h>
 #include "ffe_common.cuh"
+#include "ffe_fused_types.cuh"
 
 namespace ffe {
 
@@ -73,10 +74,35 @@ template <typename R, int C>
 int launch_psr_fixup_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, const PsrBC<R>& q, R cc, R c1, R c2,
                            R c3, bool incr, int stage, const CEB<R>& in, const CEB<R>& en, const CEB<R>& b0,
                            bool has_b0, const EB<R>& out, R ct, R* s1, R* s2, cudaStream_t st);
-// The two TMA tensor maps (OLD box, EN box) of one field array at `base`.
-int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es);
-// Tile shape the fused kernel uses (for reporting).
+// The two TMA tensor maps (OLD box, EN box) of one field array at `base`, for
+// the fused kernels of tile height ty (8 or 16).
+int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es, int ty);
+// Tile shape the single-grid fused kernel uses (for reporting).
 void fused_tile_shape(int* tx, int* ty);
+// Default z-planes per block of the fused kernel for a grid and tile height.
+int fused_planes_per_block(const Geom& g, int ty);
+
+// ---- batched launches (ffe_fused.cu with FFE_BATCH_TY = 8 / 16) ------------
+// One SSP-RK3 stage of up to BATCH_MAX grids in one launch: `grid` blocks
+// take the nitems work items (device memory; grid < nitems: persistent
+// blocks).  T: one entry per grid, passed as the kernel's parameter.  (R, C)
+// in {(float,0), (float,1), (double,0)}; double only with tile height 8.
+template <typename R, int C>
+int launch_fused_batch_t8(bool stage1, const BatchItem* items, int nitems, const BoxTable<R>& T, int grid,
+                          cudaStream_t st);
+template <typename R, int C>
+int launch_fused_batch_t16(bool stage1, const BatchItem* items, int nitems, const BoxTable<R>& T, int grid,
+                           cudaStream_t st);
+// Raise the shared-memory limit of the batched stage kernels (call before any
+// launch or capture); returns their resident blocks per SM (0 on failure).
+template <typename R, int C> int fused_batch_prepare_t8();
+template <typename R, int C> int fused_batch_prepare_t16();
+// Pulsar fix-up (update, BC, clean) of many grids; items over each grid's U box.
+template <typename R, int C>
+int launch_fix_batch(bool stage1, const FixItem* items, int nitems, const FixParams<R>* fp, cudaStream_t st);
+// user_uniform ghost planes of many grids (items: grid, x block, y block, plane).
+template <typename R>
+int launch_uniform_ghosts_batch(const FixItem* items, int nitems, const BoxTable<R>& T, cudaStream_t st);
 
 // Record a failure without a handle (read back by ffe_last_error(NULL, ...)).
 int set_thread_error(int status, const char* msg);

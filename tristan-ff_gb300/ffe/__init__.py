@@ -60,6 +60,8 @@ ABI_SYMBOLS = (
     "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
     "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
     "ffe_clean_epar_noalloc",
+    "ffe_batch_create", "ffe_batch_destroy", "ffe_batch_step", "ffe_batch_set_tiling",
+    "ffe_batch_get_tiling", "ffe_batch_autotune", "ffe_batch_launches", "ffe_batch_synchronize",
 )
 
 
@@ -147,6 +149,14 @@ def load_library(path=None):
         "ffe_init_waves": [H, ctypes.POINTER(ctypes.c_double), i32, ctypes.POINTER(ctypes.c_double)],
         "ffe_clean_epar_noalloc": [i32, i32, i32, i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+        "ffe_batch_create": [ctypes.POINTER(H), ctypes.POINTER(H), i32, ctypes.c_void_p],
+        "ffe_batch_destroy": [H],
+        "ffe_batch_step": [H, i32, ctypes.POINTER(i32)],
+        "ffe_batch_set_tiling": [H, i32, i32, i32],
+        "ffe_batch_get_tiling": [H, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)],
+        "ffe_batch_autotune": [H, i32, ctypes.POINTER(dbl)],
+        "ffe_batch_launches": [H, ctypes.POINTER(i32)],
+        "ffe_batch_synchronize": [H],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -293,6 +303,71 @@ class Solver:
         if rc not in (0, -5):
             self._ck(rc, "check_finite")
         return bool(ok.value)
+
+
+class Batch:
+    """Many Solvers advanced together (ffe_batch_*): one launch per SSP-RK3
+    stage for all members, a CUDA graph per chunk of steps.  The batch does
+    not own the solvers; close it before closing them."""
+
+    def __init__(self, solvers, stream=None):
+        self.lib = solvers[0].lib
+        self.solvers = list(solvers)
+        hs = (ctypes.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        self.b = ctypes.c_void_p()
+        rc = self.lib.ffe_batch_create(ctypes.byref(self.b), hs, len(self.solvers), stream)
+        if rc != 0:
+            raise FFEError("ffe_batch_create: %s (%s)" % (_last_error(self.lib, None), STATUS.get(rc, rc)), rc)
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise FFEError("%s: %s (%s)" % (what, _last_error(self.lib, None), STATUS.get(rc, rc)), rc)
+
+    def close(self):
+        if self.b:
+            self.lib.ffe_batch_destroy(self.b)
+            self.b = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, nsteps, step0=None):
+        """Advance every member nsteps steps; step0: per-member first step (default 0)."""
+        s0 = None
+        if step0 is not None:
+            s0 = (ctypes.c_int32 * len(self.solvers))(*[int(x) for x in step0])
+        self._ck(self.lib.ffe_batch_step(self.b, int(nsteps), s0), "batch step")
+
+    def set_tiling(self, tile_y=8, planes=0, persistent=False):
+        self._ck(self.lib.ffe_batch_set_tiling(self.b, tile_y, planes, 1 if persistent else 0), "batch tiling")
+
+    def tiling(self):
+        t, k, p = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._ck(self.lib.ffe_batch_get_tiling(self.b, ctypes.byref(t), ctypes.byref(k), ctypes.byref(p)), "tiling")
+        return {"tile_y": t.value, "planes": k.value, "persistent": bool(p.value)}
+
+    def autotune(self, reps=3):
+        """Time every tiling candidate, keep the fastest; returns its ms per stage."""
+        ms = ctypes.c_double()
+        self._ck(self.lib.ffe_batch_autotune(self.b, int(reps), ctypes.byref(ms)), "autotune")
+        return ms.value
+
+    def launches(self):
+        n = ctypes.c_int32()
+        self._ck(self.lib.ffe_batch_launches(self.b, ctypes.byref(n)), "batch launches")
+        return n.value
+
+    def synchronize(self):
+        self._ck(self.lib.ffe_batch_synchronize(self.b), "batch synchronize")
 
 
 def interior(a):

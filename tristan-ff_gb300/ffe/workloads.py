@@ -87,3 +87,82 @@ def host_waves(size, bg, modes, dtype=np.float64):
                 v = v + db[c - 3]
         out[name] = v.astype(dtype)
     return out
+
+
+# ---- many-grid workloads: batched boxes and served pulsar runs --------------
+# A run spec is a dict: kind ("packet", "tube" or "psr"), size (sx, sy, sz),
+# precision and the kind's parameters; build_solver turns it into a ready
+# Solver (fields initialised, main-loop prologue done).
+
+def tube_params(size, beta):
+    """user_uniform parameters (L0, r_L0, t0, beta) of a footpoint-twisted flux
+    tube: r0 = min(sx, sy) / 8, t0 = 50 steps."""
+    return (min(size[0], size[1]) / 8.0, 1.0, 50.0, float(beta))
+
+
+def psr_params(side, incl_deg, cc=0.45):
+    """user_psr parameters (radius, inclination, period, mu scale) of a served
+    pulsar run: R = side / 10, light cylinder 5 R, period 2 pi R_LC / c."""
+    radius = side / 10.0
+    period = 2.0 * np.pi * (5.0 * radius) / cc
+    return (radius, float(incl_deg), period, 1.0)
+
+
+def batch_boxes(n=64, seed=3, lo=48, hi=160):
+    """The batched workload: n boxes with sides uniform in [lo, hi] per axis;
+    the first half Alfven packets (periodic), the rest twisted flux tubes
+    (periodic x, y; open z) with twist amplitude U[0.1, 0.5]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = []
+    for b in range(n):
+        size = tuple(int(v) for v in rng.integers(lo, hi + 1, size=3))
+        if b < n // 2:
+            specs.append({"kind": "packet", "size": size, "seed": int(rng.integers(1 << 30))})
+        else:
+            specs.append({"kind": "tube", "size": size, "beta": float(rng.uniform(0.1, 0.5))})
+    return specs
+
+
+def served_requests(n, seed=4, rate=20.0, lo=96, hi=256, steps=(200, 2000)):
+    """The served workload: Poisson arrivals (mean `rate` per second) of pulsar
+    runs, cubic side uniform in [lo, hi], inclination U[0, 90] degrees, step
+    counts uniform in `steps`.  Returns dicts with an arrival time (s)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for r in range(n):
+        t += rng.exponential(1.0 / rate)
+        side = int(rng.integers(lo, hi + 1))
+        out.append({"kind": "psr", "size": (side, side, side), "incl": float(rng.uniform(0.0, 90.0)),
+                    "steps": int(rng.integers(steps[0], steps[1] + 1)), "arrival": t, "id": r})
+    return out
+
+
+def build_solver(spec, precision, path=None, lib_path=None):
+    """A Solver for a run spec, initialised and past the main-loop prologue."""
+    import ffe
+    size = tuple(spec["size"])
+    path = ffe.PATH_AUTO if path is None else path
+    kind = spec["kind"]
+    if kind == "packet":
+        d = ffe.make_desc(size, precision=precision, path=path)
+        s = ffe.Solver(d, lib_path)
+        bg, modes, _ = alfven_packet(size, seed=spec.get("seed", 0), amp=spec.get("amp", 0.1))
+        s.init_waves(bg, modes)
+    elif kind == "tube":
+        d = ffe.make_desc(size, precision=precision, boundary=(ffe.PERIODIC, ffe.PERIODIC, ffe.OPEN),
+                          setup=ffe.SETUP_UNIFORM, params=tube_params(size, spec["beta"]), path=path)
+        s = ffe.Solver(d, lib_path)
+        s.userInitialize()
+    elif kind == "psr":
+        side = size[0]
+        buff = spec.get("absorb_buff", int(np.ceil(side * 48 / 512)))
+        d = ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
+                          setup=ffe.SETUP_PSR, params=psr_params(side, spec["incl"]), path=path,
+                          flags=ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY)
+        s = ffe.Solver(d, lib_path)
+        s.userInitialize()
+    else:
+        raise ValueError("unknown run kind %r" % kind)
+    s.mainloop_prologue()
+    return s
