@@ -52,10 +52,15 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing: run FP64, FP32 and FP32C for N steps and report their errors")
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "serve"],
                     help="grid: the single 512^3 grid (default line); batch: 64 uneven boxes, batched vs "
-                         "one grid at a time")
+                         "one grid at a time; serve: a Poisson stream of pulsar runs, continuous batching "
+                         "vs one grid at a time")
     ap.add_argument("--batch-boxes", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
+    ap.add_argument("--budget-gb", type=float, default=180.0, help="serve: HBM admission budget")
+    ap.add_argument("--epoch-steps", type=int, default=32, help="serve: steps per batched epoch at most")
+    ap.add_argument("--fp64-checks", type=int, default=2, help="serve: runs re-done in FP64 for the error")
     ap.add_argument("--oracle-steps", type=int, default=0,
                     help="with --accuracy-steps: also check the FP64 GPU path against the CPU oracle "
                          "after this many steps")
@@ -360,6 +365,57 @@ def bench_batch(args):
     }))
 
 
+def bench_serve(args):
+    """Served workload: `--requests` pulsar runs arriving as a Poisson stream
+    (20 per second; cubic sides U[96, 256], inclination U[0, 90] degrees,
+    R = side/10, light cylinder 5R, steps U[200, 2000]) served by continuous
+    batching under the HBM budget, then by the one-grid-at-a-time path on the
+    same stream.  Reports aggregate cell-updates/s and time-to-result
+    percentiles of both, and the relative L2 error of E and B of the
+    `--fp64-checks` smallest runs against the same runs in FP64."""
+    import numpy as np
+    import torch
+    import ffe
+    import build as ffe_build
+    from ffe import serve, workloads
+    torch.cuda.set_device(0)
+    ffe_build.build()
+    prec = ffe.PRECISIONS[args.precision]
+    reqs = workloads.served_requests(args.requests)
+    check = sorted(reqs, key=lambda q: q["size"][0] ** 3 * q["steps"])[:args.fp64_checks]
+    keep = {q["id"] for q in check}
+    srv = serve.Server(precision=prec, hbm_budget=args.budget_gb * 1e9, epoch_steps=args.epoch_steps,
+                       keep_results=keep)
+    recs = srv.serve(reqs)
+    served = serve.report(recs)
+    plain = serve.report(serve.serve_plain(reqs, precision=prec))
+    errs = []
+    for q in check:
+        r = next(x for x in recs if x.id == q["id"])
+        g = workloads.build_solver(q, ffe.FP64)
+        g.mainloop(q["steps"], 0)
+        g.synchronize()
+        ref = g.fields()
+        g.close()
+        e = {}
+        for name, grp in (("E", ("ex", "ey", "ez")), ("B", ("bx", "by", "bz"))):
+            x = np.concatenate([ffe.interior(ref[k]).ravel() for k in grp])
+            y = np.concatenate([ffe.interior(r.result[k]).ravel().astype(np.float64) for k in grp])
+            e[name] = float(np.linalg.norm(x - y) / np.linalg.norm(x))
+        errs.append({"id": q["id"], "side": q["size"][0], "steps": q["steps"], "rel_l2": e})
+    print(json.dumps({
+        "metric": "served aggregate cell-updates/s; p50/p99 time-to-result", "value": served["cell_updates_per_s"],
+        "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "dtype": args.precision,
+        "data": "synthetic", "served": served, "one_grid_at_a_time": plain,
+        "speedup_vs_one_at_a_time": served["cell_updates_per_s"] / plain["cell_updates_per_s"],
+        "scheduler": {"epochs": srv.epochs, "batches_built": srv.batches_built, "peak_runs": srv.peak_runs,
+                      "peak_bytes": srv.peak_bytes, "budget_bytes": srv.budget},
+        "fp64_error": errs, "gpu_launches": srv.launches,
+        "config": {"workload": "%d pulsar runs, Poisson 20/s, sides U[96,256], steps U[200,2000]" % len(reqs),
+                   "epoch_steps": args.epoch_steps},
+    }))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -370,6 +426,11 @@ def main():
         return
     if args.workload == "batch":
         bench_batch(args)
+        return
+    if args.workload == "serve":
+        if args.precision == "fp32":
+            args.precision = "fp32c"  # the served runs are quoted at <= 1e-5 against FP64
+        bench_serve(args)
         return
     import numpy as np
     import torch

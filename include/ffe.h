@@ -153,8 +153,12 @@ typedef struct {
    a single meshblock covering the global mesh, FFE_FP32, FFE_PATH_AUTO.    */
 int ffe_desc_default(ffe_grid_desc* d, int32_t sx, int32_t sy, int32_t sz);
 
-/* Allocate device state for one meshblock (all fields zero). */
+/* Allocate device state for one meshblock (all fields zero).  The arena is
+   allocated stream-ordered on the handle's stream. */
 int ffe_create(ffe_t* out, const ffe_grid_desc* desc);
+/* Device bytes ffe_create would allocate for this descriptor (no device call;
+   no counterpart in the reference: admission control of a serving loop). */
+int ffe_desc_device_bytes(const ffe_grid_desc* desc, size_t* bytes);
 int ffe_destroy(ffe_t h);
 
 /* Copy of the last error message; returns the status that produced it. */

@@ -71,3 +71,17 @@ def test_batch_entry_points_validate_arguments_without_a_gpu(lib):
     n = ctypes.c_int32()
     assert L.ffe_batch_launches(None, ctypes.byref(n)) == -1
     assert L.ffe_batch_destroy(None) == 0
+
+
+def test_footprint_query_needs_no_gpu(lib):
+    d = ffe.make_desc((64, 48, 32), precision=ffe.FP32)
+    b = ffe.desc_device_bytes(d)
+    px = (2 + 64 + 2 + 31) // 32 * 32
+    arr = (px * 52 * 36 * 4 + 255) // 256 * 256
+    assert b >= 22 * arr and b < 22 * arr + (1 << 20)
+    d64 = ffe.make_desc((64, 48, 32), precision=ffe.FP64)
+    assert ffe.desc_device_bytes(d64) > 1.5 * b  # rows padded to 128 bytes in both
+    psr = ffe.make_desc((64, 64, 64), setup=ffe.SETUP_PSR, params=(6.0, 30.0, 100.0, 1.0), boundary=(2, 2, 2))
+    assert ffe.desc_device_bytes(psr) > ffe.desc_device_bytes(ffe.make_desc((64, 64, 64)))
+    with pytest.raises(ffe.FFEError):
+        ffe.desc_device_bytes(ffe.make_desc((1, 8, 8)))

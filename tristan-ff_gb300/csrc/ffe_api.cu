@@ -57,7 +57,8 @@ struct ffe_solver {
   size_t es = 4;
   cudaStream_t st = nullptr;
   bool own_stream = false;
-  void* arena = nullptr;
+  void* arena_raw = nullptr;  // allocation (stream-ordered)
+  void* arena = nullptr;      // 256-byte aligned start inside it
   size_t arena_bytes = 0;
   void* set[3][6] = {};
   void* b0[3] = {};
@@ -467,10 +468,13 @@ int ffe_desc_default(ffe_grid_desc* d, int32_t sx, int32_t sy, int32_t sz) {
   return FFE_OK;
 }
 
-int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
-  if (!out || !din) return set_thread_err(FFE_EINVAL, "null argument");
-  *out = nullptr;
-  ffe_grid_desc d = *din;
+}  // extern "C"
+
+namespace {
+
+// Check a descriptor and apply the reference's coupling of boundaries; 0 or
+// the failing status (message in the thread's error slot).
+int validate_desc(ffe_grid_desc& d) {
   if (d.sx < FFE_NGHOST || d.sy < FFE_NGHOST || d.sz < FFE_NGHOST)
     return set_thread_err(FFE_EINVAL, "ERROR: ghost zones overflow the domain size (s=%d,%d,%d < %d)", d.sx, d.sy,
                           d.sz, FFE_NGHOST);
@@ -495,15 +499,14 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
     return set_thread_err(FFE_EINVAL, "uniform setup needs L0, r_L0, t0 > 0");
   if (d.setup == FFE_SETUP_LOOP && !(d.params[0] > 0.0))
     return set_thread_err(FFE_EINVAL, "loop setup needs L0 > 0");
+  return FFE_OK;
+}
 
-  ffe_solver* h = new (std::nothrow) ffe_solver();
-  if (!h) return set_thread_err(FFE_ENOMEM, "host allocation failed");
-  h->d = d;
-  cudaError_t e = cudaGetDevice(&h->device);
-  if (e != cudaSuccess) {
-    delete h;
-    return set_thread_err(FFE_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  }
+// Layout of a handle's arena: fills es, g, p and box_bytes from h->d and
+// returns the bytes of the arena; *abytes = bytes of one field array,
+// *pbytes = bytes of the wave-mode table.
+size_t plan_arena(ffe_solver* h, size_t* abytes, size_t* pbytes) {
+  const ffe_grid_desc& d = h->d;
   const bool dbl = d.precision == FFE_FP64;
   h->es = dbl ? 8 : 4;
   const int ox = dbl ? Layout<double>::OX : Layout<float>::OX;
@@ -521,18 +524,53 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   for (int a = 0; a < 3; ++a) p.bnd[a] = d.boundary[a];
   p.absorb_buff = d.absorb_buff;
   p.cc = d.cc;
-
-  const size_t abytes = ((size_t)g.nelem * h->es + 255) / 256 * 256;
-  size_t total = abytes * 22;
+  *abytes = ((size_t)g.nelem * h->es + 255) / 256 * 256;
+  size_t total = *abytes * 22;
+  h->box_bytes = 0;
   if (d.setup == FFE_SETUP_PSR) {
     // staged BC: 6 x box; fused fix-up: two buffers of 6 x (box + 2 cells)
     h->box_bytes = 2 * (dbl ? psr_fix_elems<double>(h) * 8 : psr_fix_elems<float>(h) * 4);
     h->box_bytes = (h->box_bytes + 255) / 256 * 256;
     total += h->box_bytes;
   }
-  const size_t pbytes = (waves_param_bytes() + 255) / 256 * 256;
-  total += pbytes;
+  *pbytes = (waves_param_bytes() + 255) / 256 * 256;
+  total += *pbytes;
   total += 256;  // flag word
+  return total;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffe_desc_device_bytes(const ffe_grid_desc* din, size_t* bytes) {
+  if (!din || !bytes) return set_thread_err(FFE_EINVAL, "null argument");
+  ffe_solver tmp;
+  tmp.d = *din;
+  int rc;
+  if ((rc = validate_desc(tmp.d))) return rc;
+  size_t ab, pb;
+  *bytes = plan_arena(&tmp, &ab, &pb);
+  return FFE_OK;
+}
+
+int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
+  if (!out || !din) return set_thread_err(FFE_EINVAL, "null argument");
+  *out = nullptr;
+  ffe_grid_desc d = *din;
+  int rc;
+  if ((rc = validate_desc(d))) return rc;
+  ffe_solver* h = new (std::nothrow) ffe_solver();
+  if (!h) return set_thread_err(FFE_ENOMEM, "host allocation failed");
+  h->d = d;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    return set_thread_err(FFE_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  }
+  size_t abytes = 0, pbytes = 0;
+  const size_t total = plan_arena(h, &abytes, &pbytes);
+  const Geom& g = h->g;
   if (d.stream) {
     h->st = (cudaStream_t)d.stream;
   } else {
@@ -543,13 +581,16 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
     }
     h->own_stream = true;
   }
-  e = cudaMalloc(&h->arena, total);
+  // Stream-ordered allocation: creating and destroying handles (a serving loop
+  // does so while other handles compute) does not synchronise the device.
+  e = cudaMallocAsync(&h->arena_raw, total + 256, h->st);
   if (e != cudaSuccess) {
     cudaGetLastError();
     if (h->own_stream) cudaStreamDestroy(h->st);
     delete h;
-    return set_thread_err(FFE_ENOMEM, "cudaMalloc(%zu bytes): %s", total, cudaGetErrorString(e));
+    return set_thread_err(FFE_ENOMEM, "cudaMallocAsync(%zu bytes): %s", total, cudaGetErrorString(e));
   }
+  h->arena = (void*)(((uintptr_t)h->arena_raw + 255) / 256 * 256);
   h->arena_bytes = total;
   char* base = (char*)h->arena;
   for (int s = 0; s < 3; ++s)
@@ -568,7 +609,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   e = cudaMemsetAsync(h->arena, 0, total, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) {
-    cudaFree(h->arena);
+    cudaFreeAsync(h->arena_raw, h->st);
+    cudaStreamSynchronize(h->st);
     if (h->own_stream) cudaStreamDestroy(h->st);
     delete h;
     return set_thread_err(FFE_ECUDA, "arena clear: %s", cudaGetErrorString(e));
@@ -579,7 +621,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
     for (int c = 0; c < 6 && h->maps_ok; ++c)
       h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es, 8) == 0;
   if (!h->maps_ok && d.path >= FFE_PATH_FUSED) {
-    cudaFree(h->arena);
+    cudaFreeAsync(h->arena_raw, h->st);
+    cudaStreamSynchronize(h->st);
     if (h->own_stream) cudaStreamDestroy(h->st);
     delete h;
     return set_thread_err(FFE_EUNSUPPORTED, "cannot encode TMA tensor maps for the fused path");
@@ -592,7 +635,10 @@ int ffe_destroy(ffe_t h) {
   if (!h) return FFE_OK;
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
-  if (h->arena) cudaFree(h->arena);
+  if (h->arena_raw) {
+    cudaFreeAsync(h->arena_raw, h->st);
+    cudaStreamSynchronize(h->st);
+  }
   if (h->own_stream) cudaStreamDestroy(h->st);
   delete h;
   return FFE_OK;

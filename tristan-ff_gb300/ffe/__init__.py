@@ -60,6 +60,7 @@ ABI_SYMBOLS = (
     "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
     "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
     "ffe_clean_epar_noalloc",
+    "ffe_desc_device_bytes",
     "ffe_batch_create", "ffe_batch_destroy", "ffe_batch_step", "ffe_batch_set_tiling",
     "ffe_batch_get_tiling", "ffe_batch_autotune", "ffe_batch_launches", "ffe_batch_synchronize",
 )
@@ -149,6 +150,7 @@ def load_library(path=None):
         "ffe_init_waves": [H, ctypes.POINTER(ctypes.c_double), i32, ctypes.POINTER(ctypes.c_double)],
         "ffe_clean_epar_noalloc": [i32, i32, i32, i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+        "ffe_desc_device_bytes": [ctypes.POINTER(GridDesc), ctypes.POINTER(szt)],
         "ffe_batch_create": [ctypes.POINTER(H), ctypes.POINTER(H), i32, ctypes.c_void_p],
         "ffe_batch_destroy": [H],
         "ffe_batch_step": [H, i32, ctypes.POINTER(i32)],
@@ -303,6 +305,16 @@ class Solver:
         if rc not in (0, -5):
             self._ck(rc, "check_finite")
         return bool(ok.value)
+
+
+def desc_device_bytes(desc, lib_path=None):
+    """Device bytes a Solver of this descriptor would allocate (no device call)."""
+    lib = load_library(lib_path)
+    b = ctypes.c_size_t()
+    rc = lib.ffe_desc_device_bytes(ctypes.byref(desc), ctypes.byref(b))
+    if rc != 0:
+        raise FFEError("ffe_desc_device_bytes: %s (%s)" % (_last_error(lib, None), STATUS.get(rc, rc)), rc)
+    return b.value
 
 
 class Batch:

@@ -1,0 +1,185 @@
+"""Serving loop: continuous batching of force-free runs on one GPU.
+
+No counterpart in the reference (one run per job there).  A request is a run
+spec (see workloads.build_solver) with a step count and an arrival time.
+Requests are admitted first come, first served as long as the device bytes
+of the admitted runs (ffe_desc_device_bytes) stay within the HBM budget; an
+admitted run keeps its fields on the device until it finishes.  All admitted
+runs advance together: an epoch is one batched call (ffe_batch_step: one
+launch per SSP-RK3 stage for every run, captured into a CUDA graph) of
+min(epoch_steps, fewest steps left) steps.  At each epoch boundary finished
+runs leave (their fields are copied to the host while the next epoch already
+runs on the device), newly arrived runs join, and the batch is rebuilt when
+its membership changed.
+
+`serve_plain` is the one-grid-at-a-time baseline on the same requests: each
+run alone on the single-grid fused path, in arrival order.
+
+Time-to-result of a request = from its arrival to the moment its result is
+on the host.  Times are wall-clock seconds from the start of serving.
+"""
+import time
+
+import numpy as np
+
+import ffe
+from ffe import workloads
+
+
+class Record:
+    __slots__ = ("id", "spec", "steps", "done", "solver", "bytes", "arrival", "admitted", "finished", "cells",
+                 "result")
+
+    def __init__(self, spec):
+        self.id = spec.get("id")
+        self.spec = spec
+        self.steps = int(spec["steps"])
+        self.done = 0
+        self.solver = None
+        self.bytes = 0
+        self.arrival = float(spec.get("arrival", 0.0))
+        self.admitted = None
+        self.finished = None
+        s = spec["size"]
+        self.cells = int(s[0]) * int(s[1]) * int(s[2])
+        self.result = None
+
+    def summary(self):
+        return {"id": self.id, "size": list(self.spec["size"]), "steps": self.steps, "arrival": self.arrival,
+                "admitted": self.admitted, "finished": self.finished,
+                "time_to_result": None if self.finished is None else self.finished - self.arrival}
+
+
+def _desc_bytes(spec, precision):
+    """Device bytes of a run, from the descriptor build_solver would use."""
+    size = tuple(spec["size"])
+    if spec["kind"] == "psr":
+        side = size[0]
+        buff = spec.get("absorb_buff", int(np.ceil(side * 48 / 512)))
+        d = ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
+                          setup=ffe.SETUP_PSR, params=workloads.psr_params(side, spec["incl"]))
+    elif spec["kind"] == "tube":
+        d = ffe.make_desc(size, precision=precision, boundary=(ffe.PERIODIC, ffe.PERIODIC, ffe.OPEN),
+                          setup=ffe.SETUP_UNIFORM, params=workloads.tube_params(size, spec["beta"]))
+    else:
+        d = ffe.make_desc(size, precision=precision)
+    return ffe.desc_device_bytes(d)
+
+
+def _finish(r, now, keep):
+    """Copy the run's E, B to the host (kept when `keep` is true or holds the
+    run's id), record the time, free the run's device memory."""
+    fields = r.solver.fields()
+    r.result = fields if (keep is True or (keep and r.id in keep)) else None
+    r.finished = now()
+    r.solver.close()
+    r.solver = None
+
+
+class Server:
+    """Continuous batching under an HBM budget (bytes).  keep_results: True,
+    or a set of request ids whose final fields are kept on the host."""
+
+    def __init__(self, precision=ffe.FP32C, hbm_budget=180e9, epoch_steps=32, tiling=(8, 0, False),
+                 keep_results=False, build=None, batch_cls=None):
+        self.build = build or workloads.build_solver
+        self.batch_cls = batch_cls or ffe.Batch
+        self.precision = precision
+        self.budget = float(hbm_budget)
+        self.epoch_steps = int(epoch_steps)
+        self.tiling = tuple(tiling)
+        self.keep = keep_results
+        self.epochs = 0
+        self.batches_built = 0
+        self.peak_bytes = 0
+        self.peak_runs = 0
+        self.launches = 0
+        self.log = []  # per epoch: (runs, steps, device bytes in use)
+
+    def serve(self, requests):
+        recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
+        for r in recs:
+            r.bytes = _desc_bytes(r.spec, self.precision)
+            if r.bytes > self.budget:
+                raise ffe.FFEError("request %s needs %d bytes, more than the budget" % (r.id, r.bytes), -1)
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        pending = list(recs)
+        queue, active = [], []
+        used = 0
+        batch, members = None, ()
+        leaving = []  # finished in the last epoch; copied out while the next one runs
+        while pending or queue or active or leaving:
+            t = now()
+            while pending and pending[0].arrival <= t:
+                queue.append(pending.pop(0))
+            while queue and used + queue[0].bytes <= self.budget:
+                r = queue.pop(0)
+                r.solver = self.build(r.spec, self.precision)
+                r.admitted = now()
+                used += r.bytes
+                active.append(r)
+            self.peak_bytes = max(self.peak_bytes, used)
+            self.peak_runs = max(self.peak_runs, len(active))
+            if active:
+                ids = tuple(id(r) for r in active)
+                if ids != members:
+                    if batch is not None:
+                        batch.close()
+                    batch = self.batch_cls([r.solver for r in active])
+                    batch.set_tiling(*self.tiling)
+                    members = ids
+                    self.batches_built += 1
+                n = min(self.epoch_steps, min(r.steps - r.done for r in active))
+                batch.step(n, step0=[r.done for r in active])
+                self.log.append((len(active), n, used))
+                self.launches += batch.launches() * n
+                self.epochs += 1
+            # results of the previous epoch leave while this one computes
+            for r in leaving:
+                _finish(r, now, self.keep)
+                used -= r.bytes
+            leaving = []
+            if active:
+                batch.synchronize()
+                for r in active:
+                    r.done += n
+                leaving = [r for r in active if r.done >= r.steps]
+                active = [r for r in active if r.done < r.steps]
+            elif pending and not queue:
+                time.sleep(max(0.0, pending[0].arrival - now()))
+        if batch is not None:
+            batch.close()
+        return recs
+
+
+def serve_plain(requests, precision=ffe.FP32C, keep_results=False):
+    """The one-grid-at-a-time path: each run alone (single-grid fused path,
+    ffe_step), in arrival order."""
+    recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
+    t0 = time.perf_counter()
+    now = lambda: time.perf_counter() - t0
+    for r in recs:
+        wait = r.arrival - now()
+        if wait > 0:
+            time.sleep(wait)
+        r.solver = workloads.build_solver(r.spec, precision)
+        r.admitted = now()
+        r.solver.mainloop(r.steps, 0)
+        r.solver.synchronize()
+        r.done = r.steps
+        _finish(r, now, keep_results)
+    return recs
+
+
+def report(recs):
+    """Aggregate throughput (cell-updates over the span from the first arrival
+    to the last result) and time-to-result percentiles."""
+    ttr = np.array([r.finished - r.arrival for r in recs])
+    first = min(r.arrival for r in recs)
+    last = max(r.finished for r in recs)
+    work = float(sum(r.cells * r.steps for r in recs))
+    return {"requests": len(recs), "cell_updates": work, "span_s": last - first,
+            "cell_updates_per_s": work / (last - first),
+            "time_to_result_s": {"p50": float(np.percentile(ttr, 50)), "p99": float(np.percentile(ttr, 99)),
+                                 "max": float(ttr.max())}}
