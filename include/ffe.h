@@ -26,6 +26,8 @@
  *                                     user/user_loop.F90:101-164)             ffe_user_bc
  *   m_mainloop::mainloop prologue    (src/tristanmainloop.F90:41-42)           ffe_mainloop_prologue
  *   m_mainloop::mainloop step body   (src/tristanmainloop.F90:50-84)           ffe_step
+ *   m_writeoutput::writeOutput field datasets
+ *                                    (src/io/write_output.F90:270-413)         ffe_output
  *
  * Array contract.  Host arrays passed to ffe_upload / ffe_download have the
  * reference's allocation shape (src/logistics/initialize.F90:192-199):
@@ -208,6 +210,24 @@ int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* mo
    ffe_last_error(NULL, ...).                                               */
 int ffe_clean_epar_noalloc(int32_t sx, int32_t sy, int32_t sz, int32_t precision, void* ex, void* ey, void* ez,
                            const void* bx, const void* by, const void* bz, void* stream);
+
+/* --- output -------------------------------------------------------------- */
+/* writeOutput's field datasets (src/io/write_output.F90:336-413) at every
+   istep-th node of the meshblock (:270-294): nodes i = i0 + n*istep with
+   i0 = ceil(x0/istep)*istep - x0 up to (ceil((x0+sx)/istep) - 1)*istep - x0.
+   dims = nodes along x, y, z.  (With istep = 1 the reference also writes the
+   outer ghost nodes, whose interpolation reads outside its arrays; here
+   istep = 1 gives the interior nodes.) */
+int ffe_output_dims(ffe_t h, int32_t istep, int32_t dims[3]);
+/* The twelve datasets ex ey ez (interpFromEdges at offset 0), bx by bz
+   (interpFromFaces at offset 0; src/tools/helpers.F90:93-257), var1 (rho of
+   the current E at the node's cell), var2 (user_uniform: |E x B|_perp /
+   (r_perp B^2) at the cell, user/user_uniform.F90:159-170; 0 otherwise),
+   var3 (0), xx yy zz (global node coordinates), into host memory: 12 arrays
+   of dims[0]*dims[1]*dims[2] values of the storage precision, x fastest, in
+   that order.  elems must be 12 * dims[0]*dims[1]*dims[2].  Synchronises the
+   handle's stream. */
+int ffe_output(ffe_t h, int32_t istep, void* host_out, size_t elems);
 
 /* --- whole steps -------------------------------------------------------- */
 /* exchangeFields(exchangeB0=.true.) then userFieldBoundaryConditions(0). */

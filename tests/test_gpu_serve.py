@@ -45,7 +45,7 @@ def test_runs_overlap_and_all_finish(served):
     reqs, srv, recs = served
     assert len(recs) == len(reqs) and all(r.result is not None for r in recs)
     assert srv.peak_runs >= 2 and srv.batches_built >= 2
-    assert all(used <= srv.budget for _, _, used in srv.log)
+    assert all(used <= srv.budget for _, _, used, _ in srv.log)
     rep = serve.report(recs)
     assert rep["cell_updates_per_s"] > 0 and rep["time_to_result_s"]["p99"] >= rep["time_to_result_s"]["p50"]
 

@@ -68,8 +68,8 @@ def test_admission_budget_and_completion():
     for r in recs:
         assert r.result == {"steps": r.steps}, "every run gets exactly its steps"
         assert r.admitted >= r.arrival - 1e-9 and r.finished >= r.admitted
-    assert all(used <= budget for _, _, used in srv.log)
-    assert all(0 < n <= 16 for _, n, _ in srv.log)
+    assert all(used <= budget for _, _, used, _ in srv.log)
+    assert all(0 < n <= 16 for _, n, _, _ in srv.log)
     assert srv.peak_runs >= 2, "runs overlap on the device"
     # first come, first served: admission order follows arrival order
     order = sorted(recs, key=lambda r: r.admitted)
@@ -95,3 +95,18 @@ def test_served_workload_is_seeded():
     assert a == b
     assert all(96 <= q["size"][0] <= 256 and 200 <= q["steps"] <= 2000 and 0 <= q["incl"] <= 90 for q in a)
     assert all(x["arrival"] < y["arrival"] for x, y in zip(a, a[1:]))
+
+
+def test_cell_cap_limits_concurrency():
+    reqs = requests(rate=1e6)
+    cells = [q["size"][0] ** 3 for q in reqs]
+    cap = 2 * max(cells)
+    srv = serve.Server(hbm_budget=1e15, epoch_steps=16, max_active_cells=cap,
+                       build=lambda spec, prec: FakeSolver(spec), batch_cls=FakeBatch)
+    recs = srv.serve(reqs)
+    assert all(c <= cap for _, _, _, c in srv.log)
+    assert all(r.finished is not None for r in recs)
+    # a run larger than the cap still runs, alone
+    srv = serve.Server(hbm_budget=1e15, max_active_cells=1, build=lambda s, p: FakeSolver(s), batch_cls=FakeBatch)
+    recs = srv.serve(reqs[:3])
+    assert all(n == 1 for n, _, _, _ in srv.log) and all(r.finished is not None for r in recs)

@@ -824,6 +824,44 @@ int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* mo
   return check_launch(h, "init_waves");
 }
 
+int ffe_output_dims(ffe_t h, int32_t istep, int32_t dims[3]) {
+  if (!h || !dims) return set_thread_err(FFE_EINVAL, "null argument");
+  if (istep < 1) return fail(h, FFE_EINVAL, "output istep must be >= 1");
+  const NodeGrid n = node_grid(h->g, h->p, istep);
+  dims[0] = n.nx;
+  dims[1] = n.ny;
+  dims[2] = n.nz;
+  return FFE_OK;
+}
+
+int ffe_output(ffe_t h, int32_t istep, void* host_out, size_t elems) {
+  int rc;
+  if ((rc = check_handle(h))) return rc;
+  if (istep < 1) return fail(h, FFE_EINVAL, "output istep must be >= 1");
+  const NodeGrid n = node_grid(h->g, h->p, istep);
+  const size_t nn = (size_t)n.nx * n.ny * n.nz;
+  if (!host_out || elems != 12 * nn)
+    return fail(h, FFE_EINVAL, "output: need 12 * %d * %d * %d = %zu elements, got %zu", n.nx, n.ny, n.nz, 12 * nn,
+                elems);
+  if (!nn) return FFE_OK;
+  void* dbuf = nullptr;
+  FFE_CUDA(h, cudaMallocAsync(&dbuf, 12 * nn * h->es, h->st));
+  const bool v2 = h->d.setup == FFE_SETUP_UNIFORM;
+  if (h->d.precision == FFE_FP64)
+    launch_node_output<double>(h->g, h->p, n, v2, ceb_of<double>(h, h->cur), (double*)dbuf, h->st);
+  else
+    launch_node_output<float>(h->g, h->p, n, v2, ceb_of<float>(h, h->cur), (float*)dbuf, h->st);
+  rc = check_launch(h, "node output");
+  cudaError_t e = cudaSuccess;
+  if (!rc) e = cudaMemcpyAsync(host_out, dbuf, 12 * nn * h->es, cudaMemcpyDeviceToHost, h->st);
+  cudaFreeAsync(dbuf, h->st);
+  cudaError_t e2 = cudaStreamSynchronize(h->st);
+  if (rc) return rc;
+  if (e != cudaSuccess || e2 != cudaSuccess)
+    return fail(h, FFE_ECUDA, "output copy: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+  return FFE_OK;
+}
+
 // A fused-stage block that gave up waiting for its TMA copies leaves a 1 in
 // the handle's error word; report it (and clear it) once the stream is idle.
 static int check_device_error(ffe_t h) {

@@ -104,6 +104,18 @@ int launch_fix_batch(bool stage1, const FixItem* items, int nitems, const FixPar
 template <typename R>
 int launch_uniform_ghosts_batch(const FixItem* items, int nitems, const BoxTable<R>& T, cudaStream_t st);
 
+// ---- node output (ffe_output.cu) ------------------------------------------
+// Output nodes of a meshblock: i = i0 + i1 * istep for i1 < nx (same in y, z).
+struct NodeGrid {
+  int istep, i0, j0, k0, nx, ny, nz;
+};
+NodeGrid node_grid(const Geom& g, const Phys& p, int istep);
+// The twelve datasets of writeOutput at the nodes of n into out (device,
+// 12 * nx * ny * nz values, dataset-major, x fastest).
+template <typename R>
+void launch_node_output(const Geom& g, const Phys& p, const NodeGrid& n, bool var2_uniform, const CEB<R>& f, R* out,
+                        cudaStream_t st);
+
 // Record a failure without a handle (read back by ffe_last_error(NULL, ...)).
 int set_thread_error(int status, const char* msg);
 

@@ -60,7 +60,7 @@ ABI_SYMBOLS = (
     "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
     "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
     "ffe_clean_epar_noalloc",
-    "ffe_desc_device_bytes",
+    "ffe_desc_device_bytes", "ffe_output_dims", "ffe_output",
     "ffe_batch_create", "ffe_batch_destroy", "ffe_batch_step", "ffe_batch_set_tiling",
     "ffe_batch_get_tiling", "ffe_batch_autotune", "ffe_batch_launches", "ffe_batch_synchronize",
 )
@@ -151,6 +151,8 @@ def load_library(path=None):
         "ffe_clean_epar_noalloc": [i32, i32, i32, i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
         "ffe_desc_device_bytes": [ctypes.POINTER(GridDesc), ctypes.POINTER(szt)],
+        "ffe_output_dims": [H, i32, ctypes.POINTER(i32)],
+        "ffe_output": [H, i32, ctypes.c_void_p, szt],
         "ffe_batch_create": [ctypes.POINTER(H), ctypes.POINTER(H), i32, ctypes.c_void_p],
         "ffe_batch_destroy": [H],
         "ffe_batch_step": [H, i32, ctypes.POINTER(i32)],
@@ -299,6 +301,19 @@ class Solver:
         self._ck(self.lib.ffe_init_waves(self.h, bgv, m.shape[0],
                                          m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "init_waves")
 
+    def output_dims(self, istep=1):
+        d = (ctypes.c_int32 * 3)()
+        self._ck(self.lib.ffe_output_dims(self.h, int(istep), d), "output_dims")
+        return tuple(d)
+
+    def output(self, istep=1):
+        """writeOutput's twelve node datasets (OUTPUT_VARS), each shaped
+        (nz, ny, nx) with x fastest, at every istep-th node."""
+        nx, ny, nz = self.output_dims(istep)
+        a = np.empty((12, nz, ny, nx), self.dtype)
+        self._ck(self.lib.ffe_output(self.h, int(istep), a.ctypes.data, a.size), "output")
+        return {name: a[v] for v, name in enumerate(OUTPUT_VARS)}
+
     def check_finite(self):
         ok = ctypes.c_int32()
         rc = self.lib.ffe_check_finite(self.h, ctypes.byref(ok))
@@ -315,6 +330,21 @@ def desc_device_bytes(desc, lib_path=None):
     if rc != 0:
         raise FFEError("ffe_desc_device_bytes: %s (%s)" % (_last_error(lib, None), STATUS.get(rc, rc)), rc)
     return b.value
+
+
+# dataset names of the reference's field output (src/io/write_output.F90:48-51)
+OUTPUT_VARS = ("ex", "ey", "ez", "bx", "by", "bz", "var1", "var2", "var3", "xx", "yy", "zz")
+
+
+def write_output(path, step, datasets, params=None):
+    """Store one output step: the twelve datasets plus `timestep` (and the
+    run's parameters as `group:name` entries) in an .npz file, the place of
+    the reference's flds.tot.NNNNN HDF5 file (HDF5 is not available here)."""
+    d = {name: datasets[name] for name in OUTPUT_VARS}
+    d["timestep"] = np.array([step], np.int32)
+    for k, v in (params or {}).items():
+        d[k] = np.array([v])
+    np.savez(path, **d)
 
 
 class Batch:

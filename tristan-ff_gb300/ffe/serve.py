@@ -3,8 +3,10 @@
 No counterpart in the reference (one run per job there).  A request is a run
 spec (see workloads.build_solver) with a step count and an arrival time.
 Requests are admitted first come, first served as long as the device bytes
-of the admitted runs (ffe_desc_device_bytes) stay within the HBM budget; an
-admitted run keeps its fields on the device until it finishes.  All admitted
+of the admitted runs (ffe_desc_device_bytes) stay within the HBM budget and
+their cells within `max_active_cells` (enough cells to fill the GPU: more
+runs at once add no throughput, only delay every run's result); an admitted
+run keeps its fields on the device until it finishes.  All admitted
 runs advance together: an epoch is one batched call (ffe_batch_step: one
 launch per SSP-RK3 stage for every run, captured into a CUDA graph) of
 min(epoch_steps, fewest steps left) steps.  At each epoch boundary finished
@@ -81,11 +83,12 @@ class Server:
     or a set of request ids whose final fields are kept on the host."""
 
     def __init__(self, precision=ffe.FP32C, hbm_budget=180e9, epoch_steps=32, tiling=(8, 0, False),
-                 keep_results=False, build=None, batch_cls=None):
+                 keep_results=False, build=None, batch_cls=None, max_active_cells=64 << 20):
         self.build = build or workloads.build_solver
         self.batch_cls = batch_cls or ffe.Batch
         self.precision = precision
         self.budget = float(hbm_budget)
+        self.max_cells = int(max_active_cells)
         self.epoch_steps = int(epoch_steps)
         self.tiling = tuple(tiling)
         self.keep = keep_results
@@ -94,7 +97,7 @@ class Server:
         self.peak_bytes = 0
         self.peak_runs = 0
         self.launches = 0
-        self.log = []  # per epoch: (runs, steps, device bytes in use)
+        self.log = []  # per epoch: (runs, steps, device bytes in use, cells in the batch)
 
     def serve(self, requests):
         recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
@@ -107,17 +110,20 @@ class Server:
         pending = list(recs)
         queue, active = [], []
         used = 0
+        cells = 0
         batch, members = None, ()
         leaving = []  # finished in the last epoch; copied out while the next one runs
         while pending or queue or active or leaving:
             t = now()
             while pending and pending[0].arrival <= t:
                 queue.append(pending.pop(0))
-            while queue and used + queue[0].bytes <= self.budget:
+            while queue and used + queue[0].bytes <= self.budget and (
+                    not active or cells + queue[0].cells <= self.max_cells):
                 r = queue.pop(0)
                 r.solver = self.build(r.spec, self.precision)
                 r.admitted = now()
                 used += r.bytes
+                cells += r.cells
                 active.append(r)
             self.peak_bytes = max(self.peak_bytes, used)
             self.peak_runs = max(self.peak_runs, len(active))
@@ -132,7 +138,7 @@ class Server:
                     self.batches_built += 1
                 n = min(self.epoch_steps, min(r.steps - r.done for r in active))
                 batch.step(n, step0=[r.done for r in active])
-                self.log.append((len(active), n, used))
+                self.log.append((len(active), n, used, cells))
                 self.launches += batch.launches() * n
                 self.epochs += 1
             # results of the previous epoch leave while this one computes
@@ -146,6 +152,7 @@ class Server:
                     r.done += n
                 leaving = [r for r in active if r.done >= r.steps]
                 active = [r for r in active if r.done < r.steps]
+                cells -= sum(r.cells for r in leaving)
             elif pending and not queue:
                 time.sleep(max(0.0, pending[0].arrival - now()))
         if batch is not None:
