@@ -133,6 +133,14 @@ typedef enum {
    drives B to zero at the box corners, so a run with FFE_FLAG_ABSORB_CLAMP
    needs this flag to stay finite.                                          */
 #define FFE_FLAG_CLEAN_TINY 2
+/* Opt-in deviation: measure the absorbing shell's radius with the cell's own
+   y coordinate.  The reference uses jg = i + y0 (field_solver.F90:211), so
+   its shell is a function of (x, x, z): cells near the y faces are not damped
+   unless x is far from the centre, and those faces act as open boundaries
+   with frozen ghosts.  For the pulsar setup that makes the y faces
+   numerically unstable: two FP64 builds that differ only in rounding drift
+   apart by 10% (relative L2 of E) within 200 steps.                       */
+#define FFE_FLAG_ABSORB_TRUE_Y 4
 
 typedef struct {
   int32_t sx, sy, sz;          /* interior cells of this meshblock           */

@@ -58,7 +58,8 @@ struct Desc {
   int absorb_buff;
   int precision;  // 0 fp64, 1 fp32, 2 fp32c
   int setup;      // 0 none, 1 psr, 2 uniform, 3 loop
-  int flags;      // 1: clamp the absorbing depth to 1 (this library's opt-in)
+  int flags;      // this library's opt-ins: 1 clamp the absorbing depth to 1, 2 TINY in
+                  // the cleaning denominators, 4 the absorbing shell's true y coordinate
   double cc;
   double params[8];
 };
@@ -318,7 +319,8 @@ struct Oracle : OracleBase {
     loop3(0, d.sx - 1, 0, d.sy - 1, 0, d.sz - 1, [&](int i, int j, int k) {
       const long s = I(i, j, k);
       const R ig = R(i + d.x0);
-      const R jg = R(i + d.y0);  // the reference uses i here (field_solver.F90:211)
+      // the reference uses i here (field_solver.F90:211); flag 4 = this library's opt-in true y
+      const R jg = R(((d.flags & 4) ? j : i) + d.y0);
       const R kg = R(k + d.z0);
       for (int c = 0; c < 6; ++c) f[c][s] = combine(c1, c2, c3, fn[c][s], f[c][s], df[c][s], incr);
       R r = std::sqrt(((ig - xc) * (ig - xc) + (jg - yc) * (jg - yc)) + (kg - zc) * (kg - zc));

@@ -225,7 +225,9 @@ def test_large_grid_fp32_vs_fp64_gpu():
 
 @pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("bnd,flags", [((0, 0, 0), 0),
-                                       ((2, 2, 2), ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY)])
+                                       ((2, 2, 2), ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY),
+                                       ((2, 2, 2), ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY |
+                                        ffe.FLAG_ABSORB_TRUE_Y)])
 def test_psr_fused_equals_staged(prec, bnd, flags):
     """The rotating-conductor BC on the fused path (fused stage + box fix-up)
     gives the staged path's result bit for bit when both skip contraction."""
@@ -276,3 +278,20 @@ def test_uniform_fused_equals_staged(prec):
     for k in F6:
         a, b = res[ffe.PATH_STAGED][k], res[ffe.PATH_FUSED_EXACT][k]
         assert np.array_equal(a, b), (k, int(np.sum(a != b)), np.argwhere(a != b)[:3].tolist())
+
+
+@pytest.mark.parametrize("path", [ffe.PATH_STAGED, ffe.PATH_FUSED_EXACT])
+def test_true_y_absorber_bit_exact(oracle_mod, path):
+    """FFE_FLAG_ABSORB_TRUE_Y on both exact paths against the oracle."""
+    size = (30, 26, 22)
+    flags = ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY | ffe.FLAG_ABSORB_TRUE_Y
+    d = ffe.make_desc(size, precision=ffe.FP32, boundary=(2, 2, 2), absorb_buff=6, flags=flags, path=path)
+    g = ffe.Solver(d)
+    o = oracle_mod.Oracle(d)
+    bg, modes = random_modes(size, seed=4, n=6, kmax=3, amax=0.05)[:2]
+    f = host_waves(size, bg, modes, np.float32)
+    for s in (g, o):
+        s.set_fields(f)
+        s.mainloop_prologue()
+        s.mainloop(3, 0)
+    assert_same(g, o)

@@ -255,3 +255,22 @@ def test_absorbing_corners_amplify_unless_clamped(oracle_mod):
         if flags:
             assert np.all(np.isfinite(bx))
     assert peak[0] > 1e3 * peak[ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY]
+
+
+def test_true_y_shell_damps_the_y_faces(oracle_mod):
+    """field_solver.F90:211 measures the shell with jg = i + y0: at the y = 0
+    face with x at the centre nothing is damped.  Flag 4 (true y) damps it."""
+    size = (24, 24, 24)
+    got = {}
+    for flags in (ffe.FLAG_ABSORB_CLAMP, ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_ABSORB_TRUE_Y):
+        d = ffe.make_desc(size, precision=ffe.FP64, boundary=(2, 2, 2), absorb_buff=4, flags=flags)
+        o = oracle_mod.Oracle(d)
+        one = np.ones((28, 28, 28))
+        o.set_fields({"ex": one * 0, "ey": one * 0, "ez": one * 0, "bx": one, "by": one * 0, "bz": one * 0})
+        o.rk3Update(1.0, 0.0, 0.0)  # E,B <- En,Bn (= 0 after the set-up) then the shell
+        o.set_fields({"ex": one * 0, "ey": one * 0, "ez": one * 0, "bx": one, "by": one * 0, "bz": one * 0})
+        o.initRKstep()
+        o.rk3Update(1.0, 0.0, 0.0)  # B <- Bn = 1, then damped in the shell
+        got[flags] = ffe.interior(o.download("bx"))[12, 0, 12]  # k = 12, j = 0, i = 12
+    assert got[ffe.FLAG_ABSORB_CLAMP] == 1.0
+    assert got[ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_ABSORB_TRUE_Y] < 0.5

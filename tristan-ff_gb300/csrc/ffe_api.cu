@@ -145,6 +145,7 @@ template <typename R> Absorb<R> absorb_consts(ffe_t h) {
   a.rabsorb = rmax - R(h->p.absorb_buff);
   a.buff = R(h->p.absorb_buff);
   a.clamp = (h->d.flags & FFE_FLAG_ABSORB_CLAMP) ? 1 : 0;
+  a.true_y = (h->d.flags & FFE_FLAG_ABSORB_TRUE_Y) ? 1 : 0;
   return a;
 }
 
@@ -484,7 +485,7 @@ int validate_desc(ffe_grid_desc& d) {
     return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
   if (d.setup < FFE_SETUP_NONE || d.setup > FFE_SETUP_LOOP) return set_thread_err(FFE_EINVAL, "bad setup %d", d.setup);
   if (d.path < FFE_PATH_AUTO || d.path > FFE_PATH_FUSED_EXACT) return set_thread_err(FFE_EINVAL, "bad path %d", d.path);
-  if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY)) || d.reserved)
+  if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY | FFE_FLAG_ABSORB_TRUE_Y)) || d.reserved)
     return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
   for (int a = 0; a < 3; ++a)
     if (d.boundary[a] < 0 || d.boundary[a] > 2) return set_thread_err(FFE_EINVAL, "bad boundary %d", d.boundary[a]);

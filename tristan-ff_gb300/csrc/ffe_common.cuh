@@ -53,7 +53,8 @@ template <typename R> struct CEB { const R* c[6]; };
 // Absorbing-layer constants (field_solver.F90:200-204), in precision R.
 template <typename R> struct Absorb {
   R xc, yc, zc, rabsorb, buff;
-  int clamp;  // FFE_FLAG_ABSORB_CLAMP: delta_r <- min(delta_r, 1)
+  int clamp;   // FFE_FLAG_ABSORB_CLAMP: delta_r <- min(delta_r, 1)
+  int true_y;  // FFE_FLAG_ABSORB_TRUE_Y: jg = j + y0 instead of the reference's i + y0
 };
 
 // psr boundary-condition constants (user/user_psr.F90:26-37,345-374) in R.

@@ -133,7 +133,13 @@ __device__ __forceinline__ R combine(R c1, R c2, R c3, R fn, R f, R df, bool inc
 }
 
 // Absorbing shell (field_solver.F90:210-265) applied to the six updated
-// components of local cell (i, j, k); jg uses i as the reference does (:211).
+// components of a cell at global (ig_i, jg_i, kg_i).  Callers pass
+// jg_i = i + y0 as the reference does (:211), or j + y0 under
+// FFE_FLAG_ABSORB_TRUE_Y (see shell_jg).
+// The y coordinate the shell's radius uses for local cell (i, j).
+template <typename R>
+__device__ __forceinline__ int shell_jg(const Absorb<R>& ab, int i, int j, int y0) { return (ab.true_y ? j : i) + y0; }
+
 template <typename R>
 __device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int jg_i, int kg_i, R v[6]) {
   const R ig = R(ig_i), jg = R(jg_i), kg = R(kg_i);
@@ -215,13 +221,21 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
 //   J_i    = 4 CC / (64 B^2 + 64 TINY) * Srho * (cross product of bare sums),
 //   clean:   E_i -= (S.B-sums dot) * S8 / (64 B^2 + 64 ct).
 // ---------------------------------------------------------------------------
+// The hardware square-root approximation (PTX sqrt.approx.f32; +0 -> +0),
+// for the limiter's ratio in the fast path.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <class A>
 __device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, float s4a, float s4b,
                                               float s8, float s2a, float s2b, float& ea, float& eb) {
   const float bm = s8 * s8 + 16.f * (s2a * s2a + s2b * s2b);
   const float em = 64.f * (e0 * e0) + 4.f * (s4a * s4a + s4b * s4b);
   // limiter as a select: corr = 1 leaves the values unchanged exactly
-  const float corr = em > bm ? sqrtf(__fdividef(bm, em)) : 1.f;
+  const float corr = em > bm ? sqrt_approx(__fdividef(bm, em)) : 1.f;
   ea = s4a * corr;
   eb = s4b * corr;
   return __fdividef(cc4, bm + t64) * sr;

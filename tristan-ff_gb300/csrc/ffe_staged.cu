@@ -73,7 +73,7 @@ __global__ void k_update(Geom g, Phys p, Absorb<R> ab, R c1, R c2, R c3, int inc
   R v[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) v[c] = combine<R, C>(c1, c2, c3, fn.c[c][s], f.c[c][s], df.c[c][s], incr != 0);
-  if (ABS) absorb_cell<R>(ab, i + p.x0, i + p.y0, k + p.z0, v);
+  if (ABS) absorb_cell<R>(ab, i + p.x0, shell_jg(ab, i, j, p.y0), k + p.z0, v);
 #pragma unroll
   for (int c = 0; c < 6; ++c) f.c[c][s] = v[c];
 }

@@ -38,6 +38,7 @@ SETUP_NONE, SETUP_PSR, SETUP_UNIFORM, SETUP_LOOP = 0, 1, 2, 3
 PATH_AUTO, PATH_STAGED, PATH_FUSED, PATH_FUSED_EXACT = 0, 1, 2, 3
 FLAG_ABSORB_CLAMP = 1
 FLAG_CLEAN_TINY = 2
+FLAG_ABSORB_TRUE_Y = 4
 FIELDS = ("ex", "ey", "ez", "bx", "by", "bz", "b0x", "b0y", "b0z",
           "dex", "dey", "dez", "dbx", "dby", "dbz",
           "enx", "eny", "enz", "bnx", "bny", "bnz", "rho")
