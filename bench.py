@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing: run FP64, FP32 and FP32C for N steps and report their errors")
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "serve"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "serve", "psr-accuracy"],
                     help="grid: the single 512^3 grid (default line); batch: 64 uneven boxes, batched vs "
                          "one grid at a time; serve: a Poisson stream of pulsar runs, continuous batching "
                          "vs one grid at a time")
@@ -365,6 +365,59 @@ def bench_batch(args):
     }))
 
 
+def psr_accuracy(args):
+    """Sensitivity of the served pulsar configuration (cubic side --size,
+    inclination 30 degrees, R = side/10, absorbing shell of ceil(side*48/512)
+    cells with the clamp and cleaning TINY): relative L2 of E and B of FP32,
+    FP32C and of the FP64 staged path against the FP64 fused path at several
+    step counts, with the reference's shell and with FFE_FLAG_ABSORB_TRUE_Y."""
+    import numpy as np
+    import torch
+    import ffe
+    import build as ffe_build
+    from ffe import workloads
+    torch.cuda.set_device(0)
+    ffe_build.build()
+    side = args.size
+    marks = [25, 50, 100, 200, 400]
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+
+    def err(a, b):
+        out = {}
+        for n, grp in (("E", names[:3]), ("B", names[3:])):
+            x = np.concatenate([ffe.interior(a[k]).ravel().astype(np.float64) for k in grp])
+            y = np.concatenate([ffe.interior(b[k]).ravel().astype(np.float64) for k in grp])
+            out[n] = float(np.linalg.norm(x - y) / np.linalg.norm(x))
+        return out
+
+    def make(prec, flags, path=ffe.PATH_AUTO):
+        d = ffe.make_desc((side,) * 3, precision=prec, boundary=(ffe.ABSORB,) * 3,
+                          absorb_buff=int(np.ceil(side * 48 / 512)), setup=ffe.SETUP_PSR,
+                          params=workloads.psr_params(side, 30.0), path=path, flags=flags)
+        s = ffe.Solver(d)
+        s.userInitialize()
+        s.mainloop_prologue()
+        return s
+
+    base = ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY
+    for label, flags in (("reference shell (jg = i + y0)", base), ("true-y shell", base | ffe.FLAG_ABSORB_TRUE_Y)):
+        ref = make(ffe.FP64, flags)
+        cand = {"fp32": make(ffe.FP32, flags), "fp32c": make(ffe.FP32C, flags),
+                "fp64_staged": make(ffe.FP64, flags, ffe.PATH_STAGED)}
+        done = 0
+        for m in marks:
+            for s in [ref] + list(cand.values()):
+                s.mainloop(m - done, done)
+            done = m
+            fr = ref.fields()
+            row = {"workload": "psr-accuracy", "shell": label, "side": side, "step": m}
+            for n, s in cand.items():
+                row[n] = err(fr, s.fields())
+            print(json.dumps(row), flush=True)
+        for s in [ref] + list(cand.values()):
+            s.close()
+
+
 def bench_serve(args):
     """Served workload: `--requests` pulsar runs arriving as a Poisson stream
     (20 per second; cubic sides U[96, 256], inclination U[0, 90] degrees,
@@ -389,20 +442,27 @@ def bench_serve(args):
     recs = srv.serve(reqs)
     served = serve.report(recs)
     plain = serve.report(serve.serve_plain(reqs, precision=prec))
-    errs = []
-    for q in check:
-        r = next(x for x in recs if x.id == q["id"])
-        g = workloads.build_solver(q, ffe.FP64)
-        g.mainloop(q["steps"], 0)
-        g.synchronize()
-        ref = g.fields()
-        g.close()
+    def rel(ref, f):
         e = {}
         for name, grp in (("E", ("ex", "ey", "ez")), ("B", ("bx", "by", "bz"))):
             x = np.concatenate([ffe.interior(ref[k]).ravel() for k in grp])
-            y = np.concatenate([ffe.interior(r.result[k]).ravel().astype(np.float64) for k in grp])
+            y = np.concatenate([ffe.interior(f[k]).ravel().astype(np.float64) for k in grp])
             e[name] = float(np.linalg.norm(x - y) / np.linalg.norm(x))
-        errs.append({"id": q["id"], "side": q["size"][0], "steps": q["steps"], "rel_l2": e})
+        return e
+
+    errs = []
+    for q in check:
+        r = next(x for x in recs if x.id == q["id"])
+        out = {}
+        for path in (ffe.PATH_FUSED, ffe.PATH_STAGED):  # the FP64 fused path, and its own spread
+            g = workloads.build_solver(q, ffe.FP64, path=path)
+            g.mainloop(q["steps"], 0)
+            g.synchronize()
+            out[path] = g.fields()
+            g.close()
+        errs.append({"id": q["id"], "side": q["size"][0], "steps": q["steps"],
+                     "rel_l2_vs_fp64": rel(out[ffe.PATH_FUSED], r.result),
+                     "fp64_staged_vs_fp64_fused": rel(out[ffe.PATH_FUSED], out[ffe.PATH_STAGED])})
     print(json.dumps({
         "metric": "served aggregate cell-updates/s; p50/p99 time-to-result", "value": served["cell_updates_per_s"],
         "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "dtype": args.precision,
@@ -426,6 +486,9 @@ def main():
         return
     if args.workload == "batch":
         bench_batch(args)
+        return
+    if args.workload == "psr-accuracy":
+        psr_accuracy(args)
         return
     if args.workload == "serve":
         if args.precision == "fp32":

@@ -64,7 +64,7 @@ namespace FFE_FUSED_NS {
 constexpr int TX = FUSED_TX;
 constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+TX+1)
 constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
-constexpr int DO = 4, DE = 2, DN = 4;    // ring depths (the march loop is unrolled by 4)
+constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
@@ -193,42 +193,61 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const unsigned bar_old = smem_u32(bars), bar_en = smem_u32(bars + DO);
 
   // ---- producer (thread 0): TMA copies of whole planes --------------------
-  // OLD plane p lives in slot (p - kb + 2) & 3, EN plane p in (p - kb + 1) & 1;
-  // the n-th plane through a slot completes that slot's barrier phase n.
-  int old_next = kb - 2, en_next = kb - 1;  // next plane to issue (thread 0)
+  // OLD plane p lives in slot (p - kb + 2) % DO, EN plane p in (p - kb + 1) % DE.
+  int old_next = kb - 2, en_next = kb - 1;
   const int old_last = ke + 1, en_last = ke;
-  auto issue_old = [&](int p) {  // thread 0, planes in order
-    if (p > old_last) return;
-    const int s = (p - kb + 2) & (DO - 1);
+  auto issue_old = [&](int p) {
+    const int s = (p - kb + 2) % DO;
     const unsigned bar = bar_old + 8 * s;
     mbar_expect_tx(bar, 6u * OW * OH * sizeof(R));
 #pragma unroll
     for (int c = 0; c < 6; ++c)
       tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), mi + c, x0, y0, p + NG, bar);
-    old_next = p + 1;
   };
   auto issue_en = [&](int p) {
-    if (STAGE1 || p > en_last) return;
-    const int s = (p - kb + 1) & (DE - 1);
+    const int s = (p - kb + 1) % DE;
     const unsigned bar = bar_en + 8 * s;
     mbar_expect_tx(bar, 6u * OW * EH * sizeof(R));
 #pragma unroll
     for (int c = 0; c < 6; ++c)
       tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), me + c, x0, y0 + 1, p + NG, bar);
-    en_next = p + 1;
   };
   if (tid == 0) {
     for (int s = 0; s < DO + DE; ++s) mbar_init(smem_u32(bars + s), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) {  // prologue fetch: OLD kb-2 .. kb+1, EN kb-1 .. kb (every slot's first use)
-    for (int q = kb - 2; q <= kb + 1; ++q) issue_old(q);
-    issue_en(kb - 1);
-    issue_en(kb);
+  if (tid == 0) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
+    for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
+    if (!STAGE1)
+      for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
   }
-  auto wait_old = [&](int slot, unsigned parity) { return mbar_wait(bar_old + 8 * slot, parity); };
-  auto wait_en = [&](int slot, unsigned parity) { return STAGE1 || mbar_wait(bar_en + 8 * slot, parity); };
+  // At the top of iteration k every thread has finished compute_new(k): the
+  // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
+  // may run to k+4 and EN to k+2.
+  auto refill = [&](int k) {
+    if (tid != 0) return;
+    while (old_next <= old_last && old_next <= k + 4) issue_old(old_next++);
+    if (!STAGE1)
+      while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
+  };
+
+  // ---- consumers: rolling ring state, uniform across the block ------------
+  // Planes are waited for in order, each exactly once.
+  int ow_slot = 0;         // slot of the next OLD plane to wait for (kb-2 first)
+  unsigned ow_par = 0;     // its phase parity
+  int ew = 0;              // EN planes waited so far (kb-1 first)
+  auto wait_old = [&]() {
+    const bool ok = mbar_wait(bar_old + 8 * ow_slot, ow_par);
+    if (++ow_slot == DO) { ow_slot = 0; ow_par ^= 1u; }
+    return ok;
+  };
+  auto wait_en = [&]() {
+    if (STAGE1) return true;
+    const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1));
+    ++ew;
+    return ok;
+  };
 
   // ---- per-thread constants --------------------------------------------------
   const int nxl = tid % NX, nyl = tid / NX;  // NEW cell of this thread (tid < NCELL)
@@ -252,14 +271,14 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
                             (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
 
-  // NEW(p): push + update on this thread's cell.  so = OLD slot of plane p-1
-  // (planes p, p+1 follow in the next slots), es / ns = EN and NEW slots of p.
-  auto compute_new = [&](int p, int so, int es, int ns) {
+  // NEW(p): push + update on this thread's cell.  so = OLD slot of plane p-1,
+  // m = p - (kb - 1) (EN slot m % 2, NEW slot m % 4).
+  auto compute_new = [&](int p, int so, int m) {
     if (tid >= NCELL) return;
-    const int s1 = (so + 1) & (DO - 1);
-    const int s2 = (so + 2) & (DO - 1);
+    const int s1 = so == DO - 1 ? 0 : so + 1;
+    const int s2 = s1 == DO - 1 ? 0 : s1 + 1;
     const R* o1 = oth + s1 * (6 * S::OLDBOX);
-    R* dst = nwth + ns * (6 * S::NEWPL);
+    R* dst = nwth + (m & (DN - 1)) * (6 * S::NEWPL);
     R v[6];
     // block-uniform common case: every cell of the region is computed
     const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
@@ -317,7 +336,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       R d[6];
       if constexpr (FD) push_cell_fast<B0>(a, cc, d);
       else push_cell<R, C, B0, SmemOld<R, TY>, false>(a, cc, d);
-      const R* e1 = enth + es * (6 * S::ENBOX);
+      const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         const R f = o1[c * S::OLDBOX];
@@ -356,13 +375,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const R* cth = nw + (ly + 1) * NX + (lx + 1);
   const long long cbase = c_in ? g.idx(ci, cj, 0) : 0;
 
-  // clean plane k; ns = NEW slot of plane k-1 (k and k+1 follow)
-  auto clean_store = [&](int k, int ns) {
+  // clean plane k (m = k - kb: NEW slots of k-1, k, k+1 are m, m+1, m+2 mod 4)
+  auto clean_store = [&](int k, int m) {
     if (!c_in) return;
     SmemNew<R, TY> a;
-    a.b[0] = cth + ns * (6 * S::NEWPL);
-    a.b[1] = cth + ((ns + 1) & (DN - 1)) * (6 * S::NEWPL);
-    a.b[2] = cth + ((ns + 2) & (DN - 1)) * (6 * S::NEWPL);
+    a.b[0] = cth + (m & (DN - 1)) * (6 * S::NEWPL);
+    a.b[1] = cth + ((m + 1) & (DN - 1)) * (6 * S::NEWPL);
+    a.b[2] = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
     R e[3];
     if constexpr (FD) clean_cell_fast(a, e, ct);
     else clean_cell<R, C, SmemNew<R, TY>, false>(a, e, ct);
@@ -387,44 +406,26 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   };
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
-  // NEW plane p lives in slot (p - kb + 1) & 3.
   // `failed` is block-uniform: every wait result goes through a barrier-OR.
-  bool failed = __syncthreads_or(!(wait_old(0, 0) & wait_old(1, 0) & wait_old(2, 0) & wait_en(0, 0)));
-  if (!failed) {  // OLD kb-2..kb and EN kb-1 have landed
-    compute_new(kb - 1, 0, 0, 0);
-    __syncthreads();
-    if (tid == 0) {  // OLD kb-2 and EN kb-1 are free
-      issue_old(kb + 2);
-      issue_en(kb + 1);
-    }
-    failed = __syncthreads_or(!(wait_old(3, 0) & wait_en(1, 0)));  // OLD kb+1, EN kb
+  bool failed = __syncthreads_or(!(wait_old() & wait_old() & wait_old() & wait_en()));  // OLD kb-2..kb, EN kb-1
+  if (!failed) {
+    compute_new(kb - 1, 0, 0);
+    failed = __syncthreads_or(!(wait_old() & wait_en()));  // OLD kb+1, EN kb
     if (!failed) {
-      compute_new(kb, 1, 1, 1);
+      compute_new(kb, 1, 1);
       __syncthreads();
-      // ---- march: one barrier per plane, unrolled by the ring depth 4 so
-      // that every slot and barrier parity is a constant.  Iteration k
-      // (m = k - kb = m0 + u): OLD k-1's slot takes OLD k+3, EN k's slot
-      // takes EN k+2; wait OLD k+2 (slot u, parity m0/4 + 1) and EN k+1
-      // (slot u & 1, parity 1 for u < 2, else 0); NEW(k+1) into slot u+2;
-      // barrier; clean plane k from NEW slots u .. u+2.
-      for (int m0 = 0; kb + m0 < ke && !failed; m0 += 4) {
-        const unsigned pold = ((unsigned)(m0 >> 2) + 1u) & 1u;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int k = kb + m0 + u;
-          if (k >= ke) break;
-          if (tid == 0) {
-            issue_old(k + 3);
-            issue_en(k + 2);
-          }
-          const bool late = !(wait_old(u, pold) & wait_en(u & 1, u < 2 ? 1u : 0u));
-          if (!late) compute_new(k + 1, (u + 2) & 3, u & 1, (u + 2) & 3);
-          if (__syncthreads_or(late)) {
-            failed = true;
-            break;
-          }
-          clean_store(k, u);
+      // ---- march: one barrier per plane ------------------------------------
+      int so = 2;  // OLD slot of plane k for compute_new(k+1)
+      for (int k = kb, m = 0; k < ke; ++k, ++m) {
+        refill(k);
+        const bool late = !(wait_old() & wait_en());  // OLD k+2, EN k+1
+        if (!late) compute_new(k + 1, so, m + 2);
+        if (__syncthreads_or(late)) {
+          failed = true;
+          break;
         }
+        clean_store(k, m);
+        so = so == DO - 1 ? 0 : so + 1;
       }
     }
   }
@@ -433,10 +434,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       atomicExch(P.err, 1);
       // drain the copies that may still be in flight: the last use of each slot
       for (int p = max(kb - 2, old_next - DO); p < old_next; ++p)
-        mbar_wait(bar_old + 8 * ((p - kb + 2) & (DO - 1)), (unsigned)(((p - kb + 2) / DO) & 1));
+        mbar_wait(bar_old + 8 * ((p - kb + 2) % DO), (unsigned)(((p - kb + 2) / DO) & 1));
       if (!STAGE1)
         for (int p = max(kb - 1, en_next - DE); p < en_next; ++p)
-          mbar_wait(bar_en + 8 * ((p - kb + 1) & (DE - 1)), (unsigned)(((p - kb + 1) / DE) & 1));
+          mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1));
     }
     __syncthreads();
     return false;

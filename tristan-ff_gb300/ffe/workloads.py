@@ -123,10 +123,13 @@ def batch_boxes(n=64, seed=3, lo=48, hi=160):
     return specs
 
 
-def served_requests(n, seed=4, rate=20.0, lo=96, hi=256, steps=(200, 2000)):
+def served_requests(n, seed=4, rate=20.0, lo=96, hi=256, steps=(200, 2000), shell="true_y"):
     """The served workload: Poisson arrivals (mean `rate` per second) of pulsar
     runs, cubic side uniform in [lo, hi], inclination U[0, 90] degrees, step
-    counts uniform in `steps`.  Returns dicts with an arrival time (s)."""
+    counts uniform in `steps`.  Returns dicts with an arrival time (s).
+    shell: "true_y" (the absorbing shell measured with each cell's own y,
+    FFE_FLAG_ABSORB_TRUE_Y) or "reference" (jg = i + y0, whose y faces are
+    not damped and are numerically unstable for this setup)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     t = 0.0
     out = []
@@ -134,12 +137,14 @@ def served_requests(n, seed=4, rate=20.0, lo=96, hi=256, steps=(200, 2000)):
         t += rng.exponential(1.0 / rate)
         side = int(rng.integers(lo, hi + 1))
         out.append({"kind": "psr", "size": (side, side, side), "incl": float(rng.uniform(0.0, 90.0)),
-                    "steps": int(rng.integers(steps[0], steps[1] + 1)), "arrival": t, "id": r})
+                    "steps": int(rng.integers(steps[0], steps[1] + 1)), "arrival": t, "id": r, "shell": shell})
     return out
 
 
 def build_solver(spec, precision, path=None, lib_path=None):
-    """A Solver for a run spec, initialised and past the main-loop prologue."""
+    """A Solver for a run spec, initialised and past the main-loop prologue.
+    Pulsar runs use the clamped absorbing shell with TINY in the cleaning, and
+    the true-y shell when spec["shell"] == "true_y"."""
     import ffe
     size = tuple(spec["size"])
     path = ffe.PATH_AUTO if path is None else path
@@ -157,9 +162,12 @@ def build_solver(spec, precision, path=None, lib_path=None):
     elif kind == "psr":
         side = size[0]
         buff = spec.get("absorb_buff", int(np.ceil(side * 48 / 512)))
+        flags = ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY
+        if spec.get("shell") == "true_y":
+            flags |= ffe.FLAG_ABSORB_TRUE_Y
         d = ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
                           setup=ffe.SETUP_PSR, params=psr_params(side, spec["incl"]), path=path,
-                          flags=ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY)
+                          flags=flags)
         s = ffe.Solver(d, lib_path)
         s.userInitialize()
     else:
