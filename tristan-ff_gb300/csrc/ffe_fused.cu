@@ -258,15 +258,25 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const R* oth = old + (nyl + 1) * OW + (nxl + 1);  // this cell in OLD slot 0
   const R* enth = en + nyl * OW + (nxl + 1);        // in EN slot 0
   R* nwth = nw + nyl * NX + nxl;                    // in NEW slot 0
+  // B0 is read from global memory around the cell; cells of a partial tile
+  // beyond the grid read around the nearest halo cell instead (their values
+  // are computed but never used)
   long long gbase = 0;
-  if (B0 && xy_in) gbase = g.idx(gi, gj, 0);
-  // the whole 34x10 region lies in [-1, s] and needs no frozen ghost in x, y
-  const bool simple_xy = x0 + TX <= g.sx && y0 + TY <= g.sy &&
-                         (per_x || (x0 >= 1 && x0 + TX + 1 <= g.sx)) &&
+  if (B0) gbase = g.idx(min(max(gi, -1), g.sx), min(max(gj, -1), g.sy), 0);
+  // No cell of the 34x10 region is a frozen ghost in x, y: every axis is
+  // periodic or the region lies inside [-1, s].  On a periodic axis a partial
+  // tile qualifies too: its cells beyond the halo (index > s) compute values
+  // from the zero-filled or padded part of the boxes that no cleaning reads.
+  const bool simple_xy = (per_x || (x0 >= 1 && x0 + TX + 1 <= g.sx)) &&
                          (per_y || (y0 >= 1 && y0 + TY + 1 <= g.sy));
-  // periodic and open axes together: edge tiles and edge planes go cell by cell
+  // periodic and open axes together: a halo cell outside a periodic face whose
+  // image lies next to an open face takes the per-cell path (see below); such
+  // cells exist only where the tile (or plane) touches a periodic face and
+  // reaches an open face's boundary layer
   const bool mixed = (per_x || per_y || per_z) && !(per_x && per_y && per_z);
-  const bool edge_xy = x0 == 0 || x0 + TX >= g.sx || y0 == 0 || y0 + TY >= g.sy;
+  const bool touch_per_xy = (per_x && (x0 == 0 || x0 + TX >= g.sx)) || (per_y && (y0 == 0 || y0 + TY >= g.sy));
+  const bool near_open_xy = (!per_x && (x0 <= 1 || x0 + TX >= g.sx - 1)) ||
+                            (!per_y && (y0 <= 1 || y0 + TY >= g.sy - 1));
   // no cell of the tile has a periodic image in x or y
   const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
                             (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
@@ -282,7 +292,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     R v[6];
     // block-uniform common case: every cell of the region is computed
     const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
-                          !(mixed && (edge_xy || p <= 0 || p >= g.sz - 1));
+                          !(mixed && (touch_per_xy || (per_z && (p < 0 || p >= g.sz))) &&
+                            (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1))));
     bool push = true, frozen_cell = false;
     if (!all_push) {
       const bool in_range = xy_in && p >= -1 && p <= g.sz;
