@@ -65,7 +65,7 @@ constexpr int TX = FUSED_TX;
 constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+TX+1)
 constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
 constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
-constexpr long long WAIT_LIMIT = 1LL << 20;
+constexpr long long WAIT_LIMIT = 1LL << 22;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
 // rows (y0-1 .. y0+TY), NEW planes of NY rows, one thread per NEW cell
@@ -125,34 +125,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// The same probe, letting the hardware suspend the thread for up to `ns`
-// nanoseconds while the phase is pending (it returns as soon as it completes),
-// so that waiting warps leave the issue slots to the others.
-__device__ __forceinline__ bool mbar_try_wait_for(unsigned bar, unsigned parity, unsigned ns) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity), "r"(ns)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: true when the phase completed (one probe in the common case;
-// at most WAIT_LIMIT suspended probes of <= 1 us each otherwise)
+// bounded wait: true when the phase completed (one probe in the common case)
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   if (__builtin_expect(mbar_try_wait(bar, parity), 1)) return true;
   for (long long it = 1; it < WAIT_LIMIT; ++it)
-    if (mbar_try_wait_for(bar, parity, 1000u)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
   return false;
-}
-// Bring one box into L2 ahead of its load (no shared memory, no barrier).
-__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
-  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
-                   reinterpret_cast<unsigned long long>(map)),
-               "r"(x), "r"(y), "r"(z)
-               : "memory");
 }
 __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map, int x, int y, int z, unsigned bar) {
   asm volatile(
@@ -239,26 +217,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // L2 prefetch of the planes the ring takes next: OLD runs two planes and EN
-  // two planes beyond what is in shared memory or in flight.
-  auto prefetch_old = [&](int p) {
-    if (p > old_last) return;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) tma_prefetch_3d(mi + c, x0, y0, p + NG);
-  };
-  auto prefetch_en = [&](int p) {
-    if constexpr (!STAGE1) {
-      if (p > en_last) return;
-#pragma unroll
-      for (int c = 0; c < 6; ++c) tma_prefetch_3d(me + c, x0, y0 + 1, p + NG);
-    }
-  };
   if (tid == 0) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
     for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
     if (!STAGE1)
       for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
-    for (int q = kb + 3; q <= kb + 6; ++q) prefetch_old(q);
-    for (int q = kb + 1; q <= kb + 4; ++q) prefetch_en(q);
   }
   // At the top of iteration k every thread has finished compute_new(k): the
   // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
@@ -268,8 +230,6 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     while (old_next <= old_last && old_next <= k + 4) issue_old(old_next++);
     if (!STAGE1)
       while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
-    prefetch_old(k + 6);
-    prefetch_en(k + 4);
   };
 
   // ---- consumers: rolling ring state, uniform across the block ------------
