@@ -31,6 +31,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -184,8 +185,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index) if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/ffe_clocks_%d.csv" % os.getpid()
+        self.path = os.environ.get("FFE_CLOCKS_LOG") or os.path.join(
+            tempfile.gettempdir(), "ffe_clocks_rank%d_%d.csv" % (index, os.getpid()))
 
     def __enter__(self):
         try:

@@ -1,7 +1,8 @@
 """TEST INFRASTRUCTURE ONLY — ctypes wrapper of the CPU oracle (ffe_oracle.cpp).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-module, as the checker; the product path never imports it.  PARITY UNPINNED:
+module, as the reference the results are compared with; the product path never
+imports it.  PARITY UNPINNED:
 see the header of ffe_oracle.cpp.
 
 `Oracle` has the same method names as the product's `ffe.Solver`, so a test
