@@ -179,6 +179,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(nw + S::NEW);
   const Geom g = P.g;
   const int tid = threadIdx.x;
+  // the copy-issuing thread: first thread of the last warp, which has the
+  // least work (20 of its lanes compute, none cleans)
+  constexpr int PRODUCER = Tile<TY>::NT - 32;
   const int x0 = tile_x * TX, y0 = tile_y * TY;
   const int kb = chunk * P.kz;
   const int ke = min(kb + P.kz, g.sz);
@@ -212,12 +215,12 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     for (int c = 0; c < 6; ++c)
       tma_load_3d(smem_u32(en + (s * 6 + c) * S::ENBOX), me + c, x0, y0 + 1, p + NG, bar);
   };
-  if (tid == 0) {
+  if (tid == PRODUCER) {
     for (int s = 0; s < DO + DE; ++s) mbar_init(smem_u32(bars + s), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
+  if (tid == PRODUCER) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
     for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
     if (!STAGE1)
       for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
@@ -226,7 +229,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
   // may run to k+4 and EN to k+2.
   auto refill = [&](int k) {
-    if (tid != 0) return;
+    if (tid != PRODUCER) return;
     while (old_next <= old_last && old_next <= k + 4) issue_old(old_next++);
     if (!STAGE1)
       while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
@@ -441,7 +444,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     }
   }
   if (failed) {
-    if (tid == 0) {
+    if (tid == PRODUCER) {
       atomicExch(P.err, 1);
       // drain the copies that may still be in flight: the last use of each slot
       for (int p = max(kb - 2, old_next - DO); p < old_next; ++p)
@@ -456,7 +459,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // Every wait of this chunk has completed: invalidate the barriers so that a
   // persistent block may initialise them again for its next work item.
   __syncthreads();
-  if (tid == 0)
+  if (tid == PRODUCER)
     for (int s = 0; s < DO + DE; ++s) mbar_inval(smem_u32(bars + s));
   return true;
 }
