@@ -151,6 +151,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world):
+    """The largest x over all ranks (the slowest rank's time); x itself on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(cells_per_rank, steps, world, seconds):
+    """Whole-job cell-updates/s: every rank advances its own grid (replicas)."""
+    return cells_per_rank * steps * world / seconds
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -541,15 +558,11 @@ def main():
         if world > 1:
             dist.barrier()
     step += args.steps
-    t_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
+    t_ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     ok = g.check_finite()
     cells = S ** 3
     ms_per_step = t_ms / args.steps
-    value = cells * args.steps * world / (t_ms / 1e3)
+    value = job_rate(cells, args.steps, world, t_ms / 1e3)
 
     # ---- end to end through the C ABI from pinned host buffers ------------
     names = ("ex", "ey", "ez", "bx", "by", "bz")
@@ -574,13 +587,9 @@ def main():
     for n in names:
         g2._ck(g2.lib.ffe_download(g2.h, ffe.FIELD_ID[n], host[n][1].ctypes.data, host[n][1].size), "download")
     g2.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     arr_bytes = host["ex"][1].nbytes
-    e2e = {"value": cells * args.steps * world / e2e_s, "unit": "cell-updates/s",
+    e2e = {"value": job_rate(cells, args.steps, world, e2e_s), "unit": "cell-updates/s",
            "h2d_bytes_per_step": 6 * arr_bytes / args.steps, "d2h_bytes_per_step": 6 * arr_bytes / args.steps,
            "note": "upload E,B + %d steps + download E,B per run, from pinned host memory" % args.steps}
     g2.close()
