@@ -66,6 +66,7 @@ struct ffe_solver {
   void* box = nullptr;
   size_t box_bytes = 0;
   void* param = nullptr;  // device copy of the wave-mode table
+  void* stage = nullptr;  // contiguous staging array for host copies (allocated on first use)
   int* dflag = nullptr;   // finite-check word
   int* derr = nullptr;    // fused-kernel timeout word
   bool maps_ok = false;   // TMA tensor maps encoded
@@ -442,6 +443,20 @@ int do_step(ffe_t h, int nsteps, int step0) {
                                     : FN<float, 0>(__VA_ARGS__))
 #define DISPATCH_R(h, FN, ...) ((h)->d.precision == FFE_FP64 ? FN<double>(__VA_ARGS__) : FN<float>(__VA_ARGS__))
 
+// The staging array of host copies: (sx+4)(sy+4)(sz+4) values, allocated
+// stream-ordered on the first upload or download and kept until destroy.
+int ensure_stage(ffe_t h) {
+  if (h->stage) return FFE_OK;
+  const size_t n = (size_t)(h->g.sx + 2 * NG) * (h->g.sy + 2 * NG) * (h->g.sz + 2 * NG);
+  cudaError_t e = cudaMallocAsync(&h->stage, n * h->es, h->st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->stage = nullptr;
+    return fail(h, FFE_ENOMEM, "staging array (%zu bytes): %s", n * h->es, cudaGetErrorString(e));
+  }
+  return FFE_OK;
+}
+
 int check_handle(ffe_t h) {
   if (!h) return set_thread_err(FFE_EINVAL, "null handle");
   cudaError_t e = cudaSetDevice(h->device);
@@ -636,6 +651,7 @@ int ffe_destroy(ffe_t h) {
   if (!h) return FFE_OK;
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->stage) cudaFreeAsync(h->stage, h->st);
   if (h->arena_raw) {
     cudaFreeAsync(h->arena_raw, h->st);
     cudaStreamSynchronize(h->st);
@@ -676,16 +692,19 @@ int ffe_upload(ffe_t h, int32_t f, const void* host, size_t n) {
   if (!host || n != need) return fail(h, FFE_EINVAL, "upload: need %zu elements, got %zu", need, n);
   void* dst = field_ptr(h, f);
   if (!dst) return fail(h, FFE_EINVAL, "upload: bad field id %d", f);
-  const size_t es = h->es;
-  const size_t row = (size_t)(h->g.sx + 2 * NG) * es;
-  FFE_CUDA(h, cudaMemcpy2DAsync((char*)dst + (h->g.ox - NG) * es, (size_t)h->g.px * es, host, row, row,
-                                (size_t)(h->g.sy + 2 * NG) * (h->g.sz + 2 * NG), cudaMemcpyHostToDevice, h->st));
+  int rc2;
+  if ((rc2 = ensure_stage(h))) return rc2;
+  // one contiguous copy at the host link's full rate, then a repack into the padded rows
+  FFE_CUDA(h, cudaMemcpyAsync(h->stage, host, need * h->es, cudaMemcpyHostToDevice, h->st));
+  if (h->es == 8) launch_repack<double>(h->g, (const double*)h->stage, (double*)dst, true, h->st);
+  else launch_repack<float>(h->g, (const float*)h->stage, (float*)dst, true, h->st);
+  if ((rc2 = check_launch(h, "upload repack"))) return rc2;
   FFE_CUDA(h, cudaStreamSynchronize(h->st));
   if (f >= FFE_B0X && f <= FFE_B0Z) {
     // B0 enters the curl only when non-zero somewhere (field_solver.F90:84-89)
     const unsigned char* b = (const unsigned char*)host;
     bool nz = false;
-    for (size_t i = 0; i < n * es && !nz; ++i) nz = b[i] != 0;
+    for (size_t i = 0; i < n * h->es && !nz; ++i) nz = b[i] != 0;
     if (nz) h->has_b0 = true;
   }
   h->ghosts_synced = false;
@@ -700,10 +719,12 @@ int ffe_download(ffe_t h, int32_t f, void* host, size_t n) {
   if (!host || n != need) return fail(h, FFE_EINVAL, "download: need %zu elements, got %zu", need, n);
   void* src = field_ptr(h, f);
   if (!src) return fail(h, FFE_EINVAL, "download: bad field id %d", f);
-  const size_t es = h->es;
-  const size_t row = (size_t)(h->g.sx + 2 * NG) * es;
-  FFE_CUDA(h, cudaMemcpy2DAsync(host, row, (const char*)src + (h->g.ox - NG) * es, (size_t)h->g.px * es, row,
-                                (size_t)(h->g.sy + 2 * NG) * (h->g.sz + 2 * NG), cudaMemcpyDeviceToHost, h->st));
+  int rc2;
+  if ((rc2 = ensure_stage(h))) return rc2;
+  if (h->es == 8) launch_repack<double>(h->g, (const double*)src, (double*)h->stage, false, h->st);
+  else launch_repack<float>(h->g, (const float*)src, (float*)h->stage, false, h->st);
+  if ((rc2 = check_launch(h, "download repack"))) return rc2;
+  FFE_CUDA(h, cudaMemcpyAsync(host, h->stage, need * h->es, cudaMemcpyDeviceToHost, h->st));
   FFE_CUDA(h, cudaStreamSynchronize(h->st));
   return FFE_OK;
 }

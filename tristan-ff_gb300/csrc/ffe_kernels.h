@@ -39,6 +39,9 @@ size_t waves_param_bytes();
 template <typename R>
 int launch_waves(const Geom& g, const Phys& p, const double bg[3], int n, const double* modes, void* dparam,
                  const EB<R>& f, cudaStream_t st);
+// Copy one array between the reference's contiguous layout and the padded one.
+template <typename R>
+void launch_repack(const Geom& g, const R* src, R* dst, bool to_padded, cudaStream_t st);
 template <typename R>
 void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
 

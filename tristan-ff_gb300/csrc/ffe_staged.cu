@@ -453,6 +453,28 @@ void launch_loop_init(const Geom& g, const Phys& p, const double prm[8], const E
   k_loop_init<R><<<grid_for(g.sx + 2 * NG, g.sy + 2 * NG, g.sz + 2 * NG, B2), B2, 0, st>>>(g, p, L, f, f0);
 }
 
+// Reference layout (rows of sx+4 elements, contiguous) <-> padded rows of px.
+template <typename R>
+__global__ void k_repack(Geom g, const R* __restrict__ src, R* __restrict__ dst, long long n, int to_padded) {
+  const long long w = g.sx + 2 * NG;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / w, i = e - r * w;
+    const long long q = r * g.px + (g.ox - NG) + i;
+    if (to_padded) dst[q] = src[e];
+    else dst[e] = src[q];
+  }
+}
+
+template <typename R>
+void launch_repack(const Geom& g, const R* src, R* dst, bool to_padded, cudaStream_t st) {
+  const long long n = (long long)(g.sx + 2 * NG) * (g.sy + 2 * NG) * (g.sz + 2 * NG);
+  const int bs = 256;
+  const long long blocks = std::min<long long>((n + bs - 1) / bs, 152LL * 64);
+  k_repack<R><<<(unsigned)blocks, bs, 0, st>>>(g, src, dst, n, to_padded ? 1 : 0);
+}
+template void launch_repack<float>(const Geom&, const float*, float*, bool, cudaStream_t);
+template void launch_repack<double>(const Geom&, const double*, double*, bool, cudaStream_t);
+
 template <typename R>
 void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st) {
   k_finite<R><<<grid_for(g.sx, g.sy, g.sz, B2), B2, 0, st>>>(g, f, bad);
