@@ -78,6 +78,17 @@ def test_admission_budget_and_completion():
     assert rep["requests"] == len(reqs) and rep["time_to_result_s"]["p99"] >= rep["time_to_result_s"]["p50"]
 
 
+def test_shortest_job_first_admits_small_runs_first():
+    reqs = requests(rate=1e6)
+    srv = serve.Server(hbm_budget=1e15, epoch_steps=16, max_active_cells=1, policy="sjf",
+                       build=lambda spec, prec: FakeSolver(spec), batch_cls=FakeBatch)
+    recs = srv.serve(reqs)
+    order = [r for r in sorted(recs, key=lambda r: r.admitted)]
+    work = [r.cells * r.steps for r in order]
+    assert work[1:] == sorted(work[1:]), "after the first admission, least work goes first"
+    assert all(r.result is None and r.finished is not None for r in recs)
+
+
 def test_oversized_request_is_refused():
     q = requests(1)
     srv = serve.Server(hbm_budget=1000.0, build=lambda s, p: FakeSolver(s), batch_cls=FakeBatch)
