@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
     ap.add_argument("--budget-gb", type=float, default=180.0, help="serve: HBM admission budget")
     ap.add_argument("--epoch-steps", type=int, default=32, help="serve: steps per batched epoch at most")
+    ap.add_argument("--max-active-cells", type=float, default=64 * 2 ** 20,
+                    help="serve: cells of the admitted runs at most")
     ap.add_argument("--fp64-checks", type=int, default=2, help="serve: runs re-done in FP64 for the error")
     ap.add_argument("--oracle-steps", type=int, default=0,
                     help="with --accuracy-steps: also check the FP64 GPU path against the CPU oracle "
@@ -456,12 +458,12 @@ def bench_serve(args):
     check = sorted(reqs, key=lambda q: q["size"][0] ** 3 * q["steps"])[:args.fp64_checks]
     keep = {q["id"] for q in check}
     srv = serve.Server(precision=prec, hbm_budget=args.budget_gb * 1e9, epoch_steps=args.epoch_steps,
-                       keep_results=keep)
+                       keep_results=keep, max_active_cells=int(args.max_active_cells))
     recs = srv.serve(reqs)
     served = serve.report(recs)
     plain = serve.report(serve.serve_plain(reqs, precision=prec))
     sjf = serve.Server(precision=prec, hbm_budget=args.budget_gb * 1e9, epoch_steps=args.epoch_steps,
-                       policy="sjf")
+                       policy="sjf", max_active_cells=int(args.max_active_cells))
     served_sjf = serve.report(sjf.serve(reqs))
     def rel(ref, f):
         e = {}
@@ -493,7 +495,7 @@ def bench_serve(args):
                       "peak_bytes": srv.peak_bytes, "budget_bytes": srv.budget},
         "fp64_error": errs, "gpu_launches": srv.launches,
         "config": {"workload": "%d pulsar runs, Poisson 20/s, sides U[96,256], steps U[200,2000]" % len(reqs),
-                   "epoch_steps": args.epoch_steps},
+                   "epoch_steps": args.epoch_steps, "max_active_cells": int(args.max_active_cells)},
     }))
 
 
@@ -583,12 +585,10 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for n in names:
-        g2.upload(n, host[n][1])
+    g2.set_fields({n: host[n][1] for n in names})        # ffe_upload_many
     g2.mainloop_prologue()
     g2.mainloop(args.steps, 0)
-    for n in names:
-        g2._ck(g2.lib.ffe_download(g2.h, ffe.FIELD_ID[n], host[n][1].ctypes.data, host[n][1].size), "download")
+    g2.download_into({n: host[n][1] for n in names})     # ffe_download_many
     g2.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     arr_bytes = host["ex"][1].nbytes

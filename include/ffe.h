@@ -183,6 +183,12 @@ int ffe_device_bytes(ffe_t h, size_t* bytes);
 int ffe_upload(ffe_t h, int32_t field, const void* host, size_t nelems);
 int ffe_download(ffe_t h, int32_t field, void* host, size_t nelems);
 
+/* Several whole arrays per call (same shape contract); the host copy of one
+   array overlaps the on-device repacking of the previous one.  B0 arrays go
+   through ffe_upload.  Both synchronise. */
+int ffe_upload_many(ffe_t h, int32_t n, const int32_t* fields, const void* const* host, size_t nelems);
+int ffe_download_many(ffe_t h, int32_t n, const int32_t* fields, void* const* host, size_t nelems);
+
 /* --- per-procedure operator API (reference order, one launch each) ---- */
 int ffe_init_rk_step(ffe_t h);
 int ffe_compute_rho(ffe_t h);

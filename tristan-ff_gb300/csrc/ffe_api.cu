@@ -67,6 +67,9 @@ struct ffe_solver {
   size_t box_bytes = 0;
   void* param = nullptr;  // device copy of the wave-mode table
   void* stage = nullptr;  // contiguous staging array for host copies (allocated on first use)
+  void* stage2 = nullptr;            // second staging array of the multi-array copies
+  cudaStream_t cst = nullptr;        // copy stream of the multi-array copies
+  cudaEvent_t cev[4] = {};           // their ordering events
   int* dflag = nullptr;   // finite-check word
   int* derr = nullptr;    // fused-kernel timeout word
   bool maps_ok = false;   // TMA tensor maps encoded
@@ -457,6 +460,26 @@ int ensure_stage(ffe_t h) {
   return FFE_OK;
 }
 
+// The second staging array, the copy stream and the events of the
+// multi-array copies (created on first use).
+int ensure_pipeline(ffe_t h) {
+  int rc;
+  if ((rc = ensure_stage(h))) return rc;
+  if (!h->stage2) {
+    const size_t n = (size_t)(h->g.sx + 2 * NG) * (h->g.sy + 2 * NG) * (h->g.sz + 2 * NG);
+    cudaError_t e = cudaMallocAsync(&h->stage2, n * h->es, h->st);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->stage2 = nullptr;
+      return fail(h, FFE_ENOMEM, "staging array (%zu bytes): %s", n * h->es, cudaGetErrorString(e));
+    }
+  }
+  if (!h->cst) FFE_CUDA(h, cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking));
+  for (int i = 0; i < 4; ++i)
+    if (!h->cev[i]) FFE_CUDA(h, cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
+  return FFE_OK;
+}
+
 int check_handle(ffe_t h) {
   if (!h) return set_thread_err(FFE_EINVAL, "null handle");
   cudaError_t e = cudaSetDevice(h->device);
@@ -651,6 +674,13 @@ int ffe_destroy(ffe_t h) {
   if (!h) return FFE_OK;
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->cst) {
+    cudaStreamSynchronize(h->cst);
+    cudaStreamDestroy(h->cst);
+  }
+  for (int i = 0; i < 4; ++i)
+    if (h->cev[i]) cudaEventDestroy(h->cev[i]);
+  if (h->stage2) cudaFreeAsync(h->stage2, h->st);
   if (h->stage) cudaFreeAsync(h->stage, h->st);
   if (h->arena_raw) {
     cudaFreeAsync(h->arena_raw, h->st);
@@ -726,6 +756,78 @@ int ffe_download(ffe_t h, int32_t f, void* host, size_t n) {
   if ((rc2 = check_launch(h, "download repack"))) return rc2;
   FFE_CUDA(h, cudaMemcpyAsync(host, h->stage, need * h->es, cudaMemcpyDeviceToHost, h->st));
   FFE_CUDA(h, cudaStreamSynchronize(h->st));
+  return FFE_OK;
+}
+
+// Several arrays: two staging arrays alternate, the host copies run on the
+// copy stream and the repacks on the handle's stream, so the copy of one array
+// overlaps the repack of the previous one.
+int ffe_upload_many(ffe_t h, int32_t n, const int32_t* fields, const void* const* host, size_t nelems) {
+  int rc;
+  if ((rc = check_handle(h))) return rc;
+  size_t need;
+  ffe_field_elems(h, &need);
+  if (n < 0 || (n > 0 && (!fields || !host)) || nelems != need)
+    return fail(h, FFE_EINVAL, "upload_many: need %zu elements per array", need);
+  for (int i = 0; i < n; ++i) {
+    if (!host[i]) return fail(h, FFE_EINVAL, "upload_many: null host array %d", i);
+    if (!field_ptr(h, fields[i])) return fail(h, FFE_EINVAL, "upload_many: bad field id %d", fields[i]);
+    if (fields[i] >= FFE_B0X && fields[i] <= FFE_B0Z)  // B0 needs the host-side zero test
+      return fail(h, FFE_EINVAL, "upload_many: upload B0 with ffe_upload");
+  }
+  if (n == 0) return FFE_OK;
+  if ((rc = ensure_pipeline(h))) return rc;
+  void* st[2] = {h->stage, h->stage2};
+  // cev[0,1]: copy into stage b done (copy stream); cev[2,3]: repack out of stage b done (handle stream)
+  FFE_CUDA(h, cudaEventRecord(h->cev[2], h->st));
+  FFE_CUDA(h, cudaEventRecord(h->cev[3], h->st));
+  for (int i = 0; i < n; ++i) {
+    const int b = i & 1;
+    FFE_CUDA(h, cudaStreamWaitEvent(h->cst, h->cev[2 + b], 0));
+    FFE_CUDA(h, cudaMemcpyAsync(st[b], host[i], need * h->es, cudaMemcpyHostToDevice, h->cst));
+    FFE_CUDA(h, cudaEventRecord(h->cev[b], h->cst));
+    FFE_CUDA(h, cudaStreamWaitEvent(h->st, h->cev[b], 0));
+    void* dst = field_ptr(h, fields[i]);
+    if (h->es == 8) launch_repack<double>(h->g, (const double*)st[b], (double*)dst, true, h->st);
+    else launch_repack<float>(h->g, (const float*)st[b], (float*)dst, true, h->st);
+    if ((rc = check_launch(h, "upload repack"))) return rc;
+    FFE_CUDA(h, cudaEventRecord(h->cev[2 + b], h->st));
+  }
+  FFE_CUDA(h, cudaStreamSynchronize(h->st));
+  h->ghosts_synced = false;
+  return FFE_OK;
+}
+
+int ffe_download_many(ffe_t h, int32_t n, const int32_t* fields, void* const* host, size_t nelems) {
+  int rc;
+  if ((rc = check_handle(h))) return rc;
+  size_t need;
+  ffe_field_elems(h, &need);
+  if (n < 0 || (n > 0 && (!fields || !host)) || nelems != need)
+    return fail(h, FFE_EINVAL, "download_many: need %zu elements per array", need);
+  for (int i = 0; i < n; ++i) {
+    if (!host[i]) return fail(h, FFE_EINVAL, "download_many: null host array %d", i);
+    if (!field_ptr(h, fields[i])) return fail(h, FFE_EINVAL, "download_many: bad field id %d", fields[i]);
+  }
+  if (n == 0) return FFE_OK;
+  if ((rc = ensure_pipeline(h))) return rc;
+  void* st[2] = {h->stage, h->stage2};
+  // cev[0,1]: pack into stage b done (handle stream); cev[2,3]: copy out of stage b done (copy stream)
+  FFE_CUDA(h, cudaEventRecord(h->cev[2], h->cst));
+  FFE_CUDA(h, cudaEventRecord(h->cev[3], h->cst));
+  for (int i = 0; i < n; ++i) {
+    const int b = i & 1;
+    FFE_CUDA(h, cudaStreamWaitEvent(h->st, h->cev[2 + b], 0));
+    const void* src = field_ptr(h, fields[i]);
+    if (h->es == 8) launch_repack<double>(h->g, (const double*)src, (double*)st[b], false, h->st);
+    else launch_repack<float>(h->g, (const float*)src, (float*)st[b], false, h->st);
+    if ((rc = check_launch(h, "download repack"))) return rc;
+    FFE_CUDA(h, cudaEventRecord(h->cev[b], h->st));
+    FFE_CUDA(h, cudaStreamWaitEvent(h->cst, h->cev[b], 0));
+    FFE_CUDA(h, cudaMemcpyAsync(host[i], st[b], need * h->es, cudaMemcpyDeviceToHost, h->cst));
+    FFE_CUDA(h, cudaEventRecord(h->cev[2 + b], h->cst));
+  }
+  FFE_CUDA(h, cudaStreamSynchronize(h->cst));
   return FFE_OK;
 }
 

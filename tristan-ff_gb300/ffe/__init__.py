@@ -61,7 +61,7 @@ ABI_SYMBOLS = (
     "ffe_mainloop_prologue", "ffe_step", "ffe_step_path", "ffe_step_launches",
     "ffe_check_finite", "ffe_synchronize", "ffe_synchronize_timeout", "ffe_init_waves",
     "ffe_clean_epar_noalloc",
-    "ffe_desc_device_bytes", "ffe_output_dims", "ffe_output",
+    "ffe_desc_device_bytes", "ffe_output_dims", "ffe_output", "ffe_upload_many", "ffe_download_many",
     "ffe_batch_create", "ffe_batch_destroy", "ffe_batch_step", "ffe_batch_set_tiling",
     "ffe_batch_get_tiling", "ffe_batch_autotune", "ffe_batch_launches", "ffe_batch_synchronize",
 )
@@ -154,6 +154,8 @@ def load_library(path=None):
         "ffe_desc_device_bytes": [ctypes.POINTER(GridDesc), ctypes.POINTER(szt)],
         "ffe_output_dims": [H, i32, ctypes.POINTER(i32)],
         "ffe_output": [H, i32, ctypes.c_void_p, szt],
+        "ffe_upload_many": [H, i32, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_void_p), szt],
+        "ffe_download_many": [H, i32, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_void_p), szt],
         "ffe_batch_create": [ctypes.POINTER(H), ctypes.POINTER(H), i32, ctypes.c_void_p],
         "ffe_batch_destroy": [H],
         "ffe_batch_step": [H, i32, ctypes.POINTER(i32)],
@@ -231,10 +233,34 @@ class Solver:
         return a
 
     def fields(self, names=("ex", "ey", "ez", "bx", "by", "bz")):
-        return {n: self.download(n) for n in names}
+        out = {n: np.empty(self.shape, self.dtype) for n in names}
+        self.download_into(out)
+        return out
+
+    def download_into(self, arrays):
+        """Download several arrays in one call into the given host arrays (dict name -> array)."""
+        names = list(arrays)
+        for n in names:
+            a = arrays[n]
+            if a.shape != self.shape or a.dtype != self.dtype or not a.flags.c_contiguous:
+                raise FFEError("download %s: need a contiguous %s array of %s" % (n, self.shape, self.dtype), -1)
+        ids = (ctypes.c_int32 * len(names))(*[FIELD_ID[n] for n in names])
+        ptrs = (ctypes.c_void_p * len(names))(*[arrays[n].ctypes.data for n in names])
+        self._ck(self.lib.ffe_download_many(self.h, len(names), ids, ptrs, int(np.prod(self.shape))), "download")
 
     def set_fields(self, d):
-        for n, a in d.items():
+        """Upload several arrays in one call (B0 arrays one by one)."""
+        b0 = {n: a for n, a in d.items() if n in ("b0x", "b0y", "b0z")}
+        rest = {n: np.ascontiguousarray(a, dtype=self.dtype) for n, a in d.items() if n not in b0}
+        for n, a in rest.items():
+            if a.shape != self.shape:
+                raise FFEError("upload %s: shape %s, need %s" % (n, a.shape, self.shape), -1)
+        if rest:
+            names = list(rest)
+            ids = (ctypes.c_int32 * len(names))(*[FIELD_ID[n] for n in names])
+            ptrs = (ctypes.c_void_p * len(names))(*[rest[n].ctypes.data for n in names])
+            self._ck(self.lib.ffe_upload_many(self.h, len(names), ids, ptrs, int(np.prod(self.shape))), "upload")
+        for n, a in b0.items():
             self.upload(n, a)
 
     def device_bytes(self):
