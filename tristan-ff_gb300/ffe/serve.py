@@ -168,16 +168,22 @@ class Server:
         return recs
 
 
-def serve_plain(requests, precision=ffe.FP32C, keep_results=False):
+def serve_plain(requests, precision=ffe.FP32C, keep_results=False, policy="fifo"):
     """The one-grid-at-a-time path: each run alone (single-grid fused path,
-    ffe_step), in arrival order."""
+    ffe_step), next in arrival order ("fifo") or, among the requests that
+    have arrived, least work first ("sjf")."""
     recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
     t0 = time.perf_counter()
     now = lambda: time.perf_counter() - t0
-    for r in recs:
-        wait = r.arrival - now()
+    pending = list(recs)
+    while pending:
+        wait = pending[0].arrival - now()
         if wait > 0:
             time.sleep(wait)
+        t = now()
+        ready = [r for r in pending if r.arrival <= t]
+        r = min(ready, key=lambda x: (x.cells * x.steps, x.arrival)) if policy == "sjf" else ready[0]
+        pending.remove(r)
         r.solver = workloads.build_solver(r.spec, precision)
         r.admitted = now()
         r.solver.mainloop(r.steps, 0)
