@@ -525,7 +525,9 @@ struct BoxAcc {  // accessor over a compact U array around a cell
 // redone on S dilated by one cell (node distance < 2R + sqrt 3), which reads
 // updated values on S dilated by two (< 2R + 2 sqrt 3).  The rest of the
 // bounding box is skipped: its fused results stand.
-constexpr float FIX_CLEAN_MARGIN = 1.8f, FIX_UPDATE_MARGIN = 3.6f;
+struct FixMargin {
+  static constexpr float clean = 1.8f, update = 3.6f;
+};
 template <typename R>
 __device__ __forceinline__ bool fix_near(const FixParams<R>& F, int i, int j, int k, float margin) {
   const R ig = R(i + F.p.x0) - F.q.xc, jg = R(j + F.p.y0) - F.q.yc, kg = R(k + F.p.z0) - F.q.zc;
@@ -538,7 +540,7 @@ __device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, i
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
   if (bi >= F.ux || bj >= F.uy || bk >= F.uz) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
-  if (!fix_near(F, i, j, k, FIX_UPDATE_MARGIN)) return;
+  if (!fix_near(F, i, j, k, FixMargin::update)) return;
   const Geom& g = F.g;
   const long long n = (long long)F.ux * F.uy * F.uz;
   const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
@@ -573,7 +575,7 @@ template <typename R>
 __device__ __forceinline__ void fix_bc_cell(const FixParams<R>& F, int bi, int bj, int bk) {
   if (bi >= F.ux || bj >= F.uy || bk >= F.uz) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
-  if (!fix_near(F, i, j, k, FIX_UPDATE_MARGIN)) return;
+  if (!fix_near(F, i, j, k, FixMargin::update)) return;
   const long long n = (long long)F.ux * F.uy * F.uz;
   const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
   const bool in_b = i >= F.q.i_lo && i <= F.q.i_hi && j >= F.q.j_lo && j <= F.q.j_hi && k >= F.q.k_lo &&
@@ -606,7 +608,7 @@ __device__ __forceinline__ void fix_clean_cell(const FixParams<R>& F, int bi, in
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   const Geom& g = F.g;
   if (i < 0 || i >= g.sx || j < 0 || j >= g.sy || k < 0 || k >= g.sz) return;
-  if (!fix_near(F, i, j, k, FIX_CLEAN_MARGIN)) return;
+  if (!fix_near(F, i, j, k, FixMargin::clean)) return;
   const long long n = (long long)F.ux * F.uy * F.uz;
   const long long o = bi + (long long)F.ux * (bj + (long long)F.uy * bk);
   BoxAcc<R> a;
