@@ -185,7 +185,8 @@ int ffe_download(ffe_t h, int32_t field, void* host, size_t nelems);
 
 /* Several whole arrays per call (same shape contract); the host copy of one
    array overlaps the on-device repacking of the previous one.  B0 arrays go
-   through ffe_upload.  Both synchronise. */
+   through ffe_upload.  Both synchronise.  (No counterpart in the reference,
+   whose fields live on the host.) */
 int ffe_upload_many(ffe_t h, int32_t n, const int32_t* fields, const void* const* host, size_t nelems);
 int ffe_download_many(ffe_t h, int32_t n, const int32_t* fields, void* const* host, size_t nelems);
 
