@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c", "fp32cd", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-precisions", action="store_true",
+                    help="skip the FP32C and FP64 timings added to the line (single GPU)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing: run FP64, FP32 and FP32C for N steps and report their errors")
@@ -546,6 +548,7 @@ def main():
     g.mainloop_prologue()
     g.synchronize()
     launches_per_step = g.step_launches()
+    path_name = "fused" if g.step_path() != ffe.PATH_STAGED else "staged"
 
     # ---- device-resident timing -------------------------------------------
     step = 0
@@ -611,6 +614,26 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "k_fused (fused stage, %d launches/step = whole step)" % launches_per_step,
             "alg_bytes_per_launch": alg_bytes_step / 3, "peak_source": peak_kind + " copy bandwidth"}
+    others = {}
+    if world == 1 and not args.no_other_precisions:
+        # the same workload in the other precisions, for the FP32-vs-FP64 comparison of the metric
+        g.close()
+        for name, k, w in (("fp32c", 10, 2), ("fp64", 4, 1)):
+            if name == args.precision:
+                continue
+            h = ffe.Solver(ffe.make_desc(size, precision=ffe.PRECISIONS[name], stream=stream.cuda_stream))
+            h.init_waves(bg, modes)
+            h.mainloop_prologue()
+            h.mainloop(w, 0)
+            h.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            h.mainloop(k, w)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / k
+            others[name] = {"value": cells / (ms / 1e3), "ms_per_step": ms, "steps": k, "warmup": w}
+            h.close()
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
@@ -622,12 +645,13 @@ def main():
            "grid": [S, S, S], "modes": 32, "kmax": 8, "amax": 0.02, "cc": 0.45, "boundary": "periodic",
            "l2": "inputs (3.3 GB per field set) larger than L2; no flush",
            "parallelism": "replicas x%d" % world if world > 1 else "single grid",
-           "path": "fused" if g.step_path() != ffe.PATH_STAGED else "staged"}
+           "path": path_name}
     line = {"metric": "cell-updates/s per RK3 step", "value": value, "unit": "cell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": "synthetic", "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "clocks": clocks, "gpu_launches": launches_per_step * args.steps, "finite": ok}
+            "clocks": clocks, "gpu_launches": launches_per_step * args.steps, "finite": ok,
+            "other_precisions": others}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
