@@ -68,19 +68,31 @@ constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
-// rows (y0-1 .. y0+TY), NEW planes of NY rows, one thread per NEW cell
-// (TY = 8: 34 x 10 = 340 cells, 352 threads).
-template <int TY>
+// rows (y0-1 .. y0+TY), NEW planes of NY rows.  Every shared plane has rows
+// of OW words.  A thread owns CPT cells stacked in y (rows CPT*q .. CPT*q +
+// CPT-1 of the NEW region for the update, of the tile for the cleaning), so
+// the per-plane bookkeeping and the neighbour loads the cells share are paid
+// once for CPT cells.  The update threads are laid out on rows of OW (thread
+// t at x = t % OW, row group q = t / OW; lanes at x >= NX have no cell), so a
+// warp reads 32 consecutive words of a plane, free of bank conflicts.
+// TY = 8, CPT = 2: 34 x 10 = 340 cells on 5 row pairs, 192 threads (128 of
+// them also clean 32 x 8).
+template <int TY, int CPT = 1>
 struct Tile {
   static constexpr int OH = TY + 4, EH = TY + 2, NY = TY + 2;
-  static constexpr int NCELL = NX * NY;
-  static constexpr int NT = (NCELL + 31) / 32 * 32;
+  static_assert(NY % CPT == 0 && TY % CPT == 0, "cells per thread must divide the tile rows");
+  static constexpr int NT = (OW * (NY / CPT) + 31) / 32 * 32;
+  static constexpr int NCLEAN = TX * TY / CPT;  // threads that clean
 };
+// cells per thread of the single-grid kernel: two in FP32, which leaves room
+// for two blocks per SM at up to 168 registers; one in FP64
+template <typename R>
+constexpr int fused_cpt() { return sizeof(R) == 4 ? 2 : 1; }
 
 template <typename R, int TY> struct Sizes {
   static constexpr int OLDBOX = ((OW * Tile<TY>::OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
   static constexpr int ENBOX = ((OW * Tile<TY>::EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
-  static constexpr int NEWPL = Tile<TY>::NY * NX;  // one component of one NEW plane
+  static constexpr int NEWPL = Tile<TY>::NY * OW;  // one component of one NEW plane
   static constexpr int OLD = DO * 6 * OLDBOX;
   static constexpr int EN = DE * 6 * ENBOX;
   static constexpr int NEW = DN * 6 * NEWPL;
@@ -159,7 +171,7 @@ template <typename R, int TY>
 struct SmemNew {
   const R* b[3];
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
-    return b[dkk + 1][c * Sizes<R, TY>::NEWPL + djj * NX + di];
+    return b[dkk + 1][c * Sizes<R, TY>::NEWPL + djj * OW + di];
   }
 };
 
@@ -167,11 +179,12 @@ struct SmemNew {
 // z-chunk `chunk`.  Shared by the single-grid kernel and the batched kernel.
 // mi / me: the six tensor maps of the stage-input and step-start sets.
 // Returns false when a wait on a copy gave up (the error word is set).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY>
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT>
 __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensorMap* me, const Params<R>& P,
                                            int tile_x, int tile_y, int chunk) {
   using S = Sizes<R, TY>;
-  constexpr int OH = Tile<TY>::OH, EH = Tile<TY>::EH, NCELL = Tile<TY>::NCELL;
+  using T = Tile<TY, CPT>;
+  constexpr int OH = T::OH, EH = T::EH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R* old = reinterpret_cast<R*>(smem_raw);
   R* en = old + S::OLD;
@@ -180,8 +193,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const Geom g = P.g;
   const int tid = threadIdx.x;
   // the copy-issuing thread: first thread of the last warp, which has the
-  // least work (20 of its lanes compute, none cleans)
-  constexpr int PRODUCER = Tile<TY>::NT - 32;
+  // least work (it cleans nothing, and part of its lanes have no cell)
+  constexpr int PRODUCER = T::NT - 32;
   const int x0 = tile_x * TX, y0 = tile_y * TY;
   const int kb = chunk * P.kz;
   const int ke = min(kb + P.kz, g.sz);
@@ -253,20 +266,22 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   };
 
   // ---- per-thread constants --------------------------------------------------
-  const int nxl = tid % NX, nyl = tid / NX;  // NEW cell of this thread (tid < NCELL)
-  const int gi = x0 - 1 + nxl, gj = y0 - 1 + nyl;
-  const bool xy_in = tid < NCELL && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
-  const bool out_x = gi < 0 || gi >= g.sx, out_y = gj < 0 || gj >= g.sy;
-  const bool out_xy_open = ((gi < 0 || gi >= g.sx) && !per_x) || ((gj < 0 || gj >= g.sy) && !per_y);
-  const R* oth = old + (nyl + 1) * OW + (nxl + 1);  // this cell in OLD slot 0
-  const R* enth = en + nyl * OW + (nxl + 1);        // in EN slot 0
-  R* nwth = nw + nyl * NX + nxl;                    // in NEW slot 0
+  // update cells of this thread: (nxl, CPT * nq + r) of the NEW region, r < CPT
+  const int nxl = tid % OW, nq = tid / OW;
+  const bool cell_thread = nxl < NX && nq < T::NY / CPT;
+  const int gi = x0 - 1 + nxl, gj0 = y0 - 1 + CPT * nq;
+  const bool out_x = gi < 0 || gi >= g.sx;
+  const R* oth = old + (CPT * nq + 1) * OW + (nxl + 1);  // cell 0 in OLD slot 0; cell r at + r * OW
+  const R* enth = en + CPT * nq * OW + (nxl + 1);        // in EN slot 0
+  R* nwth = nw + CPT * nq * OW + nxl;                    // in NEW slot 0
   // B0 is read from global memory around the cell; cells of a partial tile
   // beyond the grid read around the nearest halo cell instead (their values
   // are computed but never used)
-  long long gbase = 0;
-  if (B0) gbase = g.idx(min(max(gi, -1), g.sx), min(max(gj, -1), g.sy), 0);
-  // No cell of the 34x10 region is a frozen ghost in x, y: every axis is
+  long long gbase[CPT];
+#pragma unroll
+  for (int r = 0; r < CPT; ++r)
+    gbase[r] = B0 ? g.idx(min(max(gi, -1), g.sx), min(max(gj0 + r, -1), g.sy), 0) : 0;
+  // No cell of the 34x(TY+2) region is a frozen ghost in x, y: every axis is
   // periodic or the region lies inside [-1, s].  On a periodic axis a partial
   // tile qualifies too: its cells beyond the halo (index > s) compute values
   // from the zero-filled or padded part of the boxes that no cleaning reads.
@@ -284,139 +299,189 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
                             (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
 
-  // NEW(p): push + update on this thread's cell.  so = OLD slot of plane p-1,
-  // m = p - (kb - 1) (EN slot m % 2, NEW slot m % 4).
+  // NEW(p): push + update on this thread's cells.  so = OLD slot of plane
+  // p-1, m = p - (kb - 1) (EN slot m % 2, NEW slot m % 4).
   auto compute_new = [&](int p, int so, int m) {
-    if (tid >= NCELL) return;
+    if (!cell_thread) return;
     const int s1 = so == DO - 1 ? 0 : so + 1;
     const int s2 = s1 == DO - 1 ? 0 : s1 + 1;
+    const R* o0 = oth + so * (6 * S::OLDBOX);
     const R* o1 = oth + s1 * (6 * S::OLDBOX);
+    const R* o2 = oth + s2 * (6 * S::OLDBOX);
+    const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
     R* dst = nwth + (m & (DN - 1)) * (6 * S::NEWPL);
-    R v[6];
-    // block-uniform common case: every cell of the region is computed
-    const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
-                          !(mixed && (touch_per_xy || (per_z && (p < 0 || p >= g.sz))) &&
-                            (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1))));
-    bool push = true, frozen_cell = false;
-    if (!all_push) {
-      const bool in_range = xy_in && p >= -1 && p <= g.sz;
-      const bool out_z = p < 0 || p >= g.sz;
-      const bool frozen = out_xy_open || (out_z && !per_z);
-      frozen_cell = in_range && frozen;
-      if (!in_range || frozen) {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) v[c] = in_range ? o1[c * S::OLDBOX] : R(0);
-        push = false;
-      } else if (out_x || out_y || out_z) {
-        // A halo cell outside a periodic face is the periodic image of an
-        // interior cell.  If that cell lies next to an open face, its stencil
-        // reaches ghosts of the open face at positions whose counterparts here
-        // are ghosts of both faces, which keep their own (frozen) values: the
-        // copy at this position would differ.  Compute it at the image instead.
-        const int wi = gi < 0 ? gi + g.sx : (gi >= g.sx ? gi - g.sx : gi);
-        const int wj = gj < 0 ? gj + g.sy : (gj >= g.sy ? gj - g.sy : gj);
-        const int wk = p < 0 ? p + g.sz : (p >= g.sz ? p - g.sz : p);
-        const bool near_open = (!per_x && (wi == 0 || wi == g.sx - 1)) || (!per_y && (wj == 0 || wj == g.sy - 1)) ||
-                               (!per_z && (wk == 0 || wk == g.sz - 1));
-        if (near_open) {
-          GlobalAcc<R> a;
-          for (int c = 0; c < 6; ++c) a.f[c] = P.in_g[c];
-          a.b0 = P.b0;
-          a.s = g.idx(wi, wj, wk);
-          a.dj = g.px;
-          a.dk = g.plane;
-          R d[6];
-          if constexpr (FD) push_cell_fast<B0>(a, cc, d);
-          else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
-#pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            const R f = __ldg(P.in_g[c] + a.s);
-            const R fn = STAGE1 ? f : __ldg(P.en_g[c] + a.s);
-            v[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
-          }
-          push = false;
-        }
-      }
-    }
-    if (push) {
+    // push + update (+ absorbing shell) of cell r from the OLD and EN rings.
+    // Only shared-memory loads: the loads the CPT cells share are made once.
+    auto push_update = [&](int r, R w[6]) {
       SmemOld<R, TY> a;
-      a.b[0] = oth + so * (6 * S::OLDBOX);
-      a.b[1] = o1;
-      a.b[2] = oth + s2 * (6 * S::OLDBOX);
+      a.b[0] = o0 + r * OW;
+      a.b[1] = o1 + r * OW;
+      a.b[2] = o2 + r * OW;
       a.b0 = P.b0;
-      a.gs = gbase + (long long)p * g.plane;
+      a.gs = gbase[r] + (long long)p * g.plane;
       a.dj = g.px;
       a.dk = g.plane;
       R d[6];
       if constexpr (FD) push_cell_fast<B0>(a, cc, d);
       else push_cell<R, C, B0, SmemOld<R, TY>, false>(a, cc, d);
-      const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const R f = o1[c * S::OLDBOX];
-        const R fn = STAGE1 ? f : e1[c * S::ENBOX];
-        v[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
+        const R f = a.b[1][c * S::OLDBOX];
+        const R fn = STAGE1 ? f : e1[c * S::ENBOX + r * OW];
+        w[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
-      if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj, P.p.y0), p + P.p.z0, v);
+      if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj0 + r, P.p.y0), p + P.p.z0, w);
+    };
+    R v[CPT][6];
+    bool frozen_cell[CPT];
+    // block-uniform common case: every cell of the region is computed
+    const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
+                          !(mixed && (touch_per_xy || (per_z && (p < 0 || p >= g.sz))) &&
+                            (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1))));
+    if (all_push) {
+#pragma unroll
+      for (int r = 0; r < CPT; ++r) {
+        push_update(r, v[r]);
+        frozen_cell[r] = false;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < CPT; ++r) {
+        const int gj = gj0 + r;
+        const bool xy_in = gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
+        const bool out_y = gj < 0 || gj >= g.sy;
+        const bool out_xy_open = (out_x && !per_x) || (out_y && !per_y);
+        const bool in_range = xy_in && p >= -1 && p <= g.sz;
+        const bool out_z = p < 0 || p >= g.sz;
+        const bool frozen = out_xy_open || (out_z && !per_z);
+        frozen_cell[r] = in_range && frozen;
+        bool push = true;
+        if (!in_range || frozen) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) v[r][c] = in_range ? o1[r * OW + c * S::OLDBOX] : R(0);
+          push = false;
+        } else if (out_x || out_y || out_z) {
+          // A halo cell outside a periodic face is the periodic image of an
+          // interior cell.  If that cell lies next to an open face, its stencil
+          // reaches ghosts of the open face at positions whose counterparts here
+          // are ghosts of both faces, which keep their own (frozen) values: the
+          // copy at this position would differ.  Compute it at the image instead.
+          const int wi = gi < 0 ? gi + g.sx : (gi >= g.sx ? gi - g.sx : gi);
+          const int wj = gj < 0 ? gj + g.sy : (gj >= g.sy ? gj - g.sy : gj);
+          const int wk = p < 0 ? p + g.sz : (p >= g.sz ? p - g.sz : p);
+          const bool near_open = (!per_x && (wi == 0 || wi == g.sx - 1)) || (!per_y && (wj == 0 || wj == g.sy - 1)) ||
+                                 (!per_z && (wk == 0 || wk == g.sz - 1));
+          if (near_open) {
+            GlobalAcc<R> a;
+            for (int c = 0; c < 6; ++c) a.f[c] = P.in_g[c];
+            a.b0 = P.b0;
+            a.s = g.idx(wi, wj, wk);
+            a.dj = g.px;
+            a.dk = g.plane;
+            R d[6];
+            if constexpr (FD) push_cell_fast<B0>(a, cc, d);
+            else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+              const R f = __ldg(P.in_g[c] + a.s);
+              const R fn = STAGE1 ? f : __ldg(P.en_g[c] + a.s);
+              v[r][c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
+            }
+            push = false;
+          }
+        }
+        if (push) push_update(r, v[r]);
+      }
     }
     // Twisted-footpoint BC (user_uniform) between the update and the cleaning,
     // on the planes z_glob <= 0 and >= gsz.  Frozen ghosts take the formula at
     // their own position; a halo cell on a periodic face is the image of an
     // interior cell, which took the formula at the image position.
     if (P.ubc && (p + P.p.z0 <= 0 || p + P.p.z0 >= P.p.gsz)) {
-      int bi = gi, bj = gj;
-      if (!frozen_cell) {
-        bi = gi < 0 ? gi + g.sx : (gi >= g.sx ? gi - g.sx : gi);
-        bj = gj < 0 ? gj + g.sy : (gj >= g.sy ? gj - g.sy : gj);
+#pragma unroll
+      for (int r = 0; r < CPT; ++r) {
+        int bi = gi, bj = gj0 + r;
+        if (!frozen_cell[r]) {
+          bi = bi < 0 ? bi + g.sx : (bi >= g.sx ? bi - g.sx : bi);
+          bj = bj < 0 ? bj + g.sy : (bj >= g.sy ? bj - g.sy : bj);
+        }
+        uniform_bc_apply(P.ub, P.p, bi, bj, p, v[r][EX], v[r][EY], v[r][BZ]);
       }
-      uniform_bc_apply(P.ub, P.p, bi, bj, p, v[EX], v[EY], v[BZ]);
     }
 #pragma unroll
-    for (int c = 0; c < 6; ++c) dst[c * S::NEWPL] = v[c];
+    for (int r = 0; r < CPT; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) dst[r * OW + c * S::NEWPL] = v[r][c];
   };
 
-  const int lx = tid % TX, ly = tid / TX;  // output cell of this thread (tid < TX*TY)
-  const int ci = x0 + lx, cj = y0 + ly;
-  const bool c_in = tid < TX * TY && ci < g.sx && cj < g.sy;
+  // cleaned cells of this thread: (lx, CPT * lq + r) of the tile, tid < NCLEAN
+  const int lx = tid % TX, lq = tid / TX;
+  const bool clean_thread = tid < T::NCLEAN;
+  const int ci = x0 + lx, cj0 = y0 + CPT * lq;
   // periodic images of this column in x and y (two per axis when s < 4)
-  int xs[3] = {ci, ci, ci}, ys[3] = {cj, cj, cj};
-  int nxs = 1, nys = 1;
+  int xs[3] = {ci, ci, ci}, nxs = 1;
   if (per_x && ci < NG) xs[nxs++] = ci + g.sx;
   if (per_x && ci >= g.sx - NG) xs[nxs++] = ci - g.sx;
-  if (per_y && cj < NG) ys[nys++] = cj + g.sy;
-  if (per_y && cj >= g.sy - NG) ys[nys++] = cj - g.sy;
-  const bool xy_images = nxs > 1 || nys > 1;
-  const R* cth = nw + (ly + 1) * NX + (lx + 1);
-  const long long cbase = c_in ? g.idx(ci, cj, 0) : 0;
+  bool c_in[CPT], xy_images[CPT];
+  long long cbase[CPT];
+#pragma unroll
+  for (int r = 0; r < CPT; ++r) {
+    const int cj = cj0 + r;
+    c_in[r] = clean_thread && ci < g.sx && cj < g.sy;
+    xy_images[r] = nxs > 1 || (per_y && (cj < NG || cj >= g.sy - NG));
+    cbase[r] = c_in[r] ? g.idx(ci, cj, 0) : 0;
+  }
+  const R* cth = nw + (CPT * lq + 1) * OW + (lx + 1);
 
   // clean plane k (m = k - kb: NEW slots of k-1, k, k+1 are m, m+1, m+2 mod 4)
   auto clean_store = [&](int k, int m) {
-    if (!c_in) return;
-    SmemNew<R, TY> a;
-    a.b[0] = cth + (m & (DN - 1)) * (6 * S::NEWPL);
-    a.b[1] = cth + ((m + 1) & (DN - 1)) * (6 * S::NEWPL);
-    a.b[2] = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
-    R e[3];
-    if constexpr (FD) clean_cell_fast(a, e, ct);
-    else clean_cell<R, C, SmemNew<R, TY>, false>(a, e, ct);
-    const R v[6] = {e[0], e[1], e[2], a(BX, 0, 0, 0), a(BY, 0, 0, 0), a(BZ, 0, 0, 0)};
-    const bool z_image = per_z && (k < NG || k >= g.sz - NG);
-    if ((no_xy_images || !xy_images) && !z_image) {
-      const long long o = cbase + (long long)k * g.plane;
+    if (!clean_thread) return;
+    const R* n0 = cth + (m & (DN - 1)) * (6 * S::NEWPL);
+    const R* n1 = cth + ((m + 1) & (DN - 1)) * (6 * S::NEWPL);
+    const R* n2 = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
+    // all loads of the CPT cells first (they share neighbours), then the stores
+    R v[CPT][6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) out[c][o] = v[c];
-      return;
+    for (int r = 0; r < CPT; ++r) {
+      SmemNew<R, TY> a;
+      a.b[0] = n0 + r * OW;
+      a.b[1] = n1 + r * OW;
+      a.b[2] = n2 + r * OW;
+      R e[3];
+      if constexpr (FD) clean_cell_fast(a, e, ct);
+      else clean_cell<R, C, SmemNew<R, TY>, false>(a, e, ct);
+      v[r][0] = e[0];
+      v[r][1] = e[1];
+      v[r][2] = e[2];
+      v[r][3] = a(BX, 0, 0, 0);
+      v[r][4] = a(BY, 0, 0, 0);
+      v[r][5] = a(BZ, 0, 0, 0);
     }
-    int zs[3] = {k, k, k}, nzs = 1;
-    if (per_z && k < NG) zs[nzs++] = k + g.sz;
-    if (per_z && k >= g.sz - NG) zs[nzs++] = k - g.sz;
-    for (int a2 = 0; a2 < nzs; ++a2)
-      for (int a1 = 0; a1 < nys; ++a1)
-        for (int a0 = 0; a0 < nxs; ++a0) {
-          const long long o = g.idx(xs[a0], ys[a1], zs[a2]);
+    const bool z_image = per_z && (k < NG || k >= g.sz - NG);
 #pragma unroll
-          for (int c = 0; c < 6; ++c) out[c][o] = v[c];
-        }
+    for (int r = 0; r < CPT; ++r) {
+      if (!c_in[r]) continue;
+      if ((no_xy_images || !xy_images[r]) && !z_image) {
+        const long long o = cbase[r] + (long long)k * g.plane;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[c][o] = v[r][c];
+        continue;
+      }
+      const int cj = cj0 + r;
+      int ys[3] = {cj, cj, cj}, nys = 1;
+      if (per_y && cj < NG) ys[nys++] = cj + g.sy;
+      if (per_y && cj >= g.sy - NG) ys[nys++] = cj - g.sy;
+      int zs[3] = {k, k, k}, nzs = 1;
+      if (per_z && k < NG) zs[nzs++] = k + g.sz;
+      if (per_z && k >= g.sz - NG) zs[nzs++] = k - g.sz;
+      for (int a2 = 0; a2 < nzs; ++a2)
+        for (int a1 = 0; a1 < nys; ++a1)
+          for (int a0 = 0; a0 < nxs; ++a0) {
+            const long long o = g.idx(xs[a0], ys[a1], zs[a2]);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) out[c][o] = v[r][c];
+          }
+    }
   };
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
@@ -467,8 +532,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 #if !defined(FFE_BATCH_TY)
 // One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).  Tile height 8.
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(Tile<8>::NT) k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
-  stage_body<R, C, B0, ABS, STAGE1, 8>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
+__global__ void __launch_bounds__(Tile<8, fused_cpt<R>()>::NT, sizeof(R) == 4 ? 2 : 1)
+    k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
+  stage_body<R, C, B0, ABS, STAGE1, 8, fused_cpt<R>()>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 #else
 // Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
@@ -480,18 +546,18 @@ __global__ void __launch_bounds__(Tile<8>::NT) k_fused(const __grid_constant__ M
 // block b takes items b, b + gridDim.x, ... (the host orders items by
 // decreasing work).
 template <typename R, int C, bool STAGE1, int TY>
-__global__ void __launch_bounds__(Tile<TY>::NT, (sizeof(R) == 4 && TY == 8) ? 2 : 1)
+__global__ void __launch_bounds__(Tile<TY, fused_cpt<R>()>::NT, (sizeof(R) == 4 && TY == 8) ? 2 : 1)
     k_fused_batch(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const BatchItem it = items[w];
     const BatchBox<R>& e = T.b[it.box];
     bool ok;
     if (e.has_b0) {
-      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, true, false, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, true, false, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     } else {
-      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, false, false, STAGE1, TY>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, false, false, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     }
     if (!ok) return;
   }
@@ -741,7 +807,7 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
         return -3;                                                                               \
       attr_set = true;                                                                           \
     }                                                                                            \
-    kf<<<grid, Tile<TY>::NT, smem, st>>>(M, P);                                                  \
+    kf<<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(M, P);                                  \
   } while (0)
   if (has_b0) {
     if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
@@ -882,8 +948,8 @@ int FFE_BATCH_LAUNCH(bool stage1, const BatchItem* items, int nitems, const BoxT
   constexpr int TY = FFE_BATCH_TY;
   const size_t smem = Sizes<R, TY>::BYTES;
   if (nitems <= 0) return 0;
-  if (stage1) k_fused_batch<R, C, true, TY><<<grid, Tile<TY>::NT, smem, st>>>(items, nitems, T);
-  else k_fused_batch<R, C, false, TY><<<grid, Tile<TY>::NT, smem, st>>>(items, nitems, T);
+  if (stage1) k_fused_batch<R, C, true, TY><<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(items, nitems, T);
+  else k_fused_batch<R, C, false, TY><<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(items, nitems, T);
   return 0;
 }
 
@@ -899,8 +965,8 @@ int FFE_BATCH_PREP() {
   if (cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   if (cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   int n1 = 0, n2 = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k1, Tile<TY>::NT, smem) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k2, Tile<TY>::NT, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k1, Tile<TY, fused_cpt<R>()>::NT, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k2, Tile<TY, fused_cpt<R>()>::NT, smem) != cudaSuccess) return 0;
   return n1 < n2 ? n1 : n2;
 }
 
