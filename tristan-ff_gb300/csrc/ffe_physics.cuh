@@ -220,6 +220,12 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
 //   64 B^2 = S8^2 + 16 (S2a^2 + S2b^2),   64 E^2 = 64 e0^2 + 4 (S4a^2 + S4b^2),
 //   J_i    = 4 CC / (64 B^2 + 64 TINY) * Srho * (cross product of bare sums),
 //   clean:   E_i -= (S.B-sums dot) * S8 / (64 B^2 + 64 ct).
+// The four- and eight-term sums are added as balanced trees (dependency depth
+// 2 and 3 instead of 3 and 7) grouped by y row: the sub-sum of one row is the
+// same expression for the two cells that share the row when a thread updates
+// two cells stacked in y, so it is evaluated once.  Unlike the exact path this
+// changes the association of the reference's sums (rounding differences of
+// an ulp or so per average).
 // ---------------------------------------------------------------------------
 // The hardware square-root approximation (PTX sqrt.approx.f32; +0 -> +0),
 // for the limiter's ratio in the fast path.
@@ -229,15 +235,60 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   return r;
 }
 
+// Row-grouped partial sums of field c around the cell:
+//   xpair(c, dx, dj, dk) = F(0, dj, dk) + F(dx, dj, dk)
+//   zpair(c, dj, dz)     = F(0, dj, 0) + F(0, dj, dz)
+//   quad(c, dx, dj, dz)  = xpair(c, dx, dj, 0) + xpair(c, dx, dj, dz)
+//   oct(c, dx, dy, dz)   = quad(c, dx, 0, dz) + quad(c, dx, dy, dz)
 template <class A>
-__device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, float s4a, float s4b,
-                                              float s8, float s2a, float s2b, float& ea, float& eb) {
-  const float bm = s8 * s8 + 16.f * (s2a * s2a + s2b * s2b);
-  const float em = 64.f * (e0 * e0) + 4.f * (s4a * s4a + s4b * s4b);
+__device__ __forceinline__ float xpair(const A& a, int c, int dx, int dj, int dk) {
+  return a(c, 0, dj, dk) + a(c, dx, dj, dk);
+}
+template <class A>
+__device__ __forceinline__ float zpair(const A& a, int c, int dj, int dz) {
+  return a(c, 0, dj, 0) + a(c, 0, dj, dz);
+}
+template <class A>
+__device__ __forceinline__ float quad(const A& a, int c, int dx, int dj, int dz) {
+  return xpair(a, c, dx, dj, 0) + xpair(a, c, dx, dj, dz);
+}
+template <class A>
+__device__ __forceinline__ float oct(const A& a, int c, int dx, int dy, int dz) {
+  return quad(a, c, dx, 0, dz) + quad(a, c, dx, dy, dz);
+}
+
+// The bare sums of the averages at the three E points (field_solver.F90
+// :93-99, :116-122, :139-145 for the push; :290-295, :304-309, :318-323 for
+// the cleaning, which averages the same neighbours): the two 4-point sums of
+// the other E components (sa, sb), the 8-point sum of the B component along
+// the point (s8) and the 2-point sums of the other two B components (s2a, s2b).
+struct PointSums {
+  float sa, sb, s8, s2a, s2b;
+};
+template <class A>
+__device__ __forceinline__ PointSums sums_x(const A& a) {  // Ex point: Ey, Ez; Bx; By, Bz
+  return {xpair(a, EY, 1, 0, 0) + xpair(a, EY, 1, -1, 0), xpair(a, EZ, 1, 0, 0) + xpair(a, EZ, 1, 0, -1),
+          oct(a, BX, 1, -1, -1), a(BY, 0, 0, 0) + a(BY, 0, 0, -1), a(BZ, 0, 0, 0) + a(BZ, 0, -1, 0)};
+}
+template <class A>
+__device__ __forceinline__ PointSums sums_y(const A& a) {  // Ey point: Ex, Ez; By; Bx, Bz
+  return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 1, 0), zpair(a, EZ, 0, -1) + zpair(a, EZ, 1, -1),
+          oct(a, BY, -1, 1, -1), a(BX, 0, 0, 0) + a(BX, 0, 0, -1), a(BZ, 0, 0, 0) + a(BZ, -1, 0, 0)};
+}
+template <class A>
+__device__ __forceinline__ PointSums sums_z(const A& a) {  // Ez point: Ex, Ey; Bz; Bx, By
+  return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 0, 1), zpair(a, EY, 0, 1) + zpair(a, EY, -1, 1),
+          oct(a, BZ, -1, -1, 1), a(BX, 0, 0, 0) + a(BX, 0, -1, 0), a(BY, 0, 0, 0) + a(BY, -1, 0, 0)};
+}
+
+__device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, const PointSums& s,
+                                              float& ea, float& eb) {
+  const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+  const float em = 64.f * (e0 * e0) + 4.f * (s.sa * s.sa + s.sb * s.sb);
   // limiter as a select: corr = 1 leaves the values unchanged exactly
   const float corr = em > bm ? sqrt_approx(__fdividef(bm, em)) : 1.f;
-  ea = s4a * corr;
-  eb = s4b * corr;
+  ea = s.sa * corr;
+  eb = s.sb * corr;
   return __fdividef(cc4, bm + t64) * sr;
 }
 
@@ -259,72 +310,44 @@ __device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6])
   const float r0 = a.rho(0, 0, 0);
   const float cc4 = 4.f * cc, t64 = 64.f * tiny<float>();
   float ea, eb, k;
-  // X current at the Ex point (field_solver.F90:91-111)
-  {
-    const float sy = ((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0);
-    const float sz = ((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1);
-    const float b8 = ((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
-                       a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1);
-    const float by2 = by0 + a(BY, 0, 0, -1), bz2 = bz0 + a(BZ, 0, -1, 0);
-    k = fast_current<A>(cc4, t64, a.rho(1, 0, 0) + r0, ex0, sy, sz, b8, by2, bz2, ea, eb);
-    d[0] = -(cc * cbx) - k * (ea * bz2 - by2 * eb);
+  {  // X current at the Ex point (field_solver.F90:91-111)
+    const PointSums s = sums_x(a);
+    k = fast_current(cc4, t64, a.rho(1, 0, 0) + r0, ex0, s, ea, eb);
+    d[0] = -(cc * cbx) - k * (ea * s.s2b - s.s2a * eb);
   }
-  // Y current at the Ey point (:114-134)
-  {
-    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0);
-    const float sz = ((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1);
-    const float b8 = ((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
-                       a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1);
-    const float bx2 = bx0 + a(BX, 0, 0, -1), bz2 = bz0 + a(BZ, -1, 0, 0);
-    k = fast_current<A>(cc4, t64, a.rho(0, 1, 0) + r0, ey0, sx, sz, b8, bx2, bz2, ea, eb);
-    d[1] = -(cc * cby) - k * (eb * bx2 - ea * bz2);
+  {  // Y current at the Ey point (:114-134)
+    const PointSums s = sums_y(a);
+    k = fast_current(cc4, t64, a.rho(0, 1, 0) + r0, ey0, s, ea, eb);
+    d[1] = -(cc * cby) - k * (eb * s.s2a - ea * s.s2b);
   }
-  // Z current at the Ez point (:137-157)
-  {
-    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1);
-    const float sy = ((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1);
-    const float b8 = ((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
-                       a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1);
-    const float bx2 = bx0 + a(BX, 0, -1, 0), by2 = by0 + a(BY, -1, 0, 0);
-    k = fast_current<A>(cc4, t64, r0 + a.rho(0, 0, 1), ez0, sx, sy, b8, bx2, by2, ea, eb);
-    d[2] = -(cc * cbz) - k * (ea * by2 - bx2 * eb);
+  {  // Z current at the Ez point (:137-157)
+    const PointSums s = sums_z(a);
+    k = fast_current(cc4, t64, r0 + a.rho(0, 0, 1), ez0, s, ea, eb);
+    d[2] = -(cc * cbz) - k * (ea * s.s2b - s.s2a * eb);
   }
 }
 
 template <class A>
 __device__ __forceinline__ void clean_cell_fast(const A& a, float e[3], float ct) {
   const float ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
-  const float bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
   const float c64 = 64.f * ct;
   {  // Ex point (:289-300)
-    const float sy = ((ey0 + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0);
-    const float sz = ((ez0 + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1);
-    const float b8 = ((((((bx0 + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
-                       a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1);
-    const float b2a = by0 + a(BY, 0, 0, -1), b2b = bz0 + a(BZ, 0, -1, 0);
-    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
-    const float ep = ex0 * b8 + sy * b2a + sz * b2b;
-    e[0] = ex0 - __fdividef(ep * b8, bm + c64);
+    const PointSums s = sums_x(a);
+    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+    const float ep = ex0 * s.s8 + s.sa * s.s2a + s.sb * s.s2b;
+    e[0] = ex0 - __fdividef(ep * s.s8, bm + c64);
   }
   {  // Ey point (:303-314)
-    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0);
-    const float sz = ((ez0 + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1);
-    const float b8 = ((((((by0 + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
-                       a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1);
-    const float b2a = bx0 + a(BX, 0, 0, -1), b2b = bz0 + a(BZ, -1, 0, 0);
-    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
-    const float ep = sx * b2a + ey0 * b8 + sz * b2b;
-    e[1] = ey0 - __fdividef(ep * b8, bm + c64);
+    const PointSums s = sums_y(a);
+    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+    const float ep = s.sa * s.s2a + ey0 * s.s8 + s.sb * s.s2b;
+    e[1] = ey0 - __fdividef(ep * s.s8, bm + c64);
   }
   {  // Ez point (:317-328)
-    const float sx = ((ex0 + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1);
-    const float sy = ((ey0 + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1);
-    const float b8 = ((((((bz0 + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
-                       a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1);
-    const float b2a = bx0 + a(BX, 0, -1, 0), b2b = by0 + a(BY, -1, 0, 0);
-    const float bm = b8 * b8 + 16.f * (b2a * b2a + b2b * b2b);
-    const float ep = sx * b2a + sy * b2b + ez0 * b8;
-    e[2] = ez0 - __fdividef(ep * b8, bm + c64);
+    const PointSums s = sums_z(a);
+    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+    const float ep = s.sa * s.s2a + s.sb * s.s2b + ez0 * s.s8;
+    e[2] = ez0 - __fdividef(ep * s.s8, bm + c64);
   }
 }
 
