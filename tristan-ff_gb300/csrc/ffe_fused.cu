@@ -72,16 +72,19 @@ constexpr long long WAIT_LIMIT = 1LL << 22;
 // of OW words.  A thread owns CPT cells stacked in y (rows CPT*q .. CPT*q +
 // CPT-1 of the NEW region for the update, of the tile for the cleaning), so
 // the per-plane bookkeeping and the neighbour loads the cells share are paid
-// once for CPT cells.  The update threads are laid out on rows of OW (thread
-// t at x = t % OW, row group q = t / OW; lanes at x >= NX have no cell), so a
-// warp reads 32 consecutive words of a plane, free of bank conflicts.
+// once for CPT cells.  The update threads are laid out on rows of TP (thread
+// t at x = t % TP, row group q = t / TP; lanes at x >= NX have no cell): TP =
+// OW for two cells per thread (FP32), so that a warp's lanes fall on
+// consecutive words of a row; TP = NX for one (FP64, whose double-rate pipe
+// is the limit), so that no lane idles.
 // TY = 8, CPT = 2: 34 x 10 = 340 cells on 5 row pairs, 192 threads (128 of
-// them also clean 32 x 8).
+// them also clean 32 x 8); CPT = 1: 340 cells, 352 threads.
 template <int TY, int CPT = 1>
 struct Tile {
   static constexpr int OH = TY + 4, EH = TY + 2, NY = TY + 2;
   static_assert(NY % CPT == 0 && TY % CPT == 0, "cells per thread must divide the tile rows");
-  static constexpr int NT = (OW * (NY / CPT) + 31) / 32 * 32;
+  static constexpr int TP = CPT == 1 ? NX : OW;
+  static constexpr int NT = (TP * (NY / CPT) + 31) / 32 * 32;
   static constexpr int NCLEAN = TX * TY / CPT;  // threads that clean
 };
 // cells per thread of the single-grid kernel: two in FP32, which leaves room
@@ -267,7 +270,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 
   // ---- per-thread constants --------------------------------------------------
   // update cells of this thread: (nxl, CPT * nq + r) of the NEW region, r < CPT
-  const int nxl = tid % OW, nq = tid / OW;
+  const int nxl = tid % T::TP, nq = tid / T::TP;
   const bool cell_thread = nxl < NX && nq < T::NY / CPT;
   const int gi = x0 - 1 + nxl, gj0 = y0 - 1 + CPT * nq;
   const bool out_x = gi < 0 || gi >= g.sx;
