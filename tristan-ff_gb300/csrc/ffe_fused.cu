@@ -64,7 +64,7 @@ namespace FFE_FUSED_NS {
 constexpr int TX = FUSED_TX;
 constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+TX+1)
 constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
-constexpr int DO = 5, DE = 2, DN = 4;    // ring depths
+constexpr int DN = 4;                    // NEW ring depth
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
@@ -92,14 +92,28 @@ struct Tile {
 template <typename R>
 constexpr int fused_cpt() { return sizeof(R) == 4 ? 2 : 1; }
 
-template <typename R, int TY> struct Sizes {
+// Ring layout.  Standard (FP64, the batched kernels): OLD ring of 5 planes
+// (two planes of copies ahead of use), step-start fields in a 2-plane TMA
+// ring, NEW rows of OW words.  Lean (the single-grid FP32 kernel): OLD ring of
+// 4 planes (one plane ahead), step-start fields loaded by each thread for its
+// own cells into registers one plane ahead, NEW rows of NX words: 74 KB of
+// shared memory at TY = 8, so that three blocks fit on an SM.
+template <bool LEAN>
+struct Rings {
+  static constexpr int DO = LEAN ? 4 : 5, DE = LEAN ? 0 : 2;
+  static constexpr int NP = LEAN ? NX : OW;  // NEW row pitch
+};
+template <typename R>
+constexpr bool fused_lean() { return sizeof(R) == 4; }
+
+template <typename R, int TY, bool LEAN = false> struct Sizes {
   static constexpr int OLDBOX = ((OW * Tile<TY>::OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
   static constexpr int ENBOX = ((OW * Tile<TY>::EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
-  static constexpr int NEWPL = Tile<TY>::NY * OW;  // one component of one NEW plane
-  static constexpr int OLD = DO * 6 * OLDBOX;
-  static constexpr int EN = DE * 6 * ENBOX;
+  static constexpr int NEWPL = Tile<TY>::NY * Rings<LEAN>::NP;  // one component of one NEW plane
+  static constexpr int OLD = Rings<LEAN>::DO * 6 * OLDBOX;
+  static constexpr int EN = Rings<LEAN>::DE * 6 * ENBOX;
   static constexpr int NEW = DN * 6 * NEWPL;
-  static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * (DO + DE);
+  static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * (Rings<LEAN>::DO + Rings<LEAN>::DE);
 };
 
 // Accessor over global arrays around linear index s (used for halo cells that
@@ -170,11 +184,11 @@ struct SmemOld {
 };
 
 // Accessor over the NEW ring for clean_cell.
-template <typename R, int TY>
+template <typename R, int TY, bool LEAN>
 struct SmemNew {
   const R* b[3];
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
-    return b[dkk + 1][c * Sizes<R, TY>::NEWPL + djj * OW + di];
+    return b[dkk + 1][c * Sizes<R, TY, LEAN>::NEWPL + djj * Rings<LEAN>::NP + di];
   }
 };
 
@@ -182,11 +196,12 @@ struct SmemNew {
 // z-chunk `chunk`.  Shared by the single-grid kernel and the batched kernel.
 // mi / me: the six tensor maps of the stage-input and step-start sets.
 // Returns false when a wait on a copy gave up (the error word is set).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT>
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT, bool LEAN>
 __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensorMap* me, const Params<R>& P,
                                            int tile_x, int tile_y, int chunk) {
-  using S = Sizes<R, TY>;
+  using S = Sizes<R, TY, LEAN>;
   using T = Tile<TY, CPT>;
+  constexpr int DO = Rings<LEAN>::DO, DE = Rings<LEAN>::DE, NP = Rings<LEAN>::NP;
   constexpr int OH = T::OH, EH = T::EH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R* old = reinterpret_cast<R*>(smem_raw);
@@ -224,7 +239,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       tma_load_3d(smem_u32(old + (s * 6 + c) * S::OLDBOX), mi + c, x0, y0, p + NG, bar);
   };
   auto issue_en = [&](int p) {
-    const int s = (p - kb + 1) % DE;
+    const int s = (p - kb + 1) % (DE > 0 ? DE : 1);
     const unsigned bar = bar_en + 8 * s;
     mbar_expect_tx(bar, 6u * OW * EH * sizeof(R));
 #pragma unroll
@@ -236,18 +251,18 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == PRODUCER) {  // prologue fetch: OLD kb-2 .. kb+2, EN kb-1 .. kb
-    for (; old_next <= min(kb + 2, old_last); ++old_next) issue_old(old_next);
-    if (!STAGE1)
+  if (tid == PRODUCER) {  // prologue fetch: OLD kb-2 .. kb+DO-3, EN kb-1 .. kb
+    for (; old_next <= min(kb + DO - 3, old_last); ++old_next) issue_old(old_next);
+    if (!STAGE1 && DE > 0)
       for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
   }
-  // At the top of iteration k every thread has finished compute_new(k): the
-  // OLD slots of planes k-2, k-1 and the EN slot of plane k are free, so OLD
-  // may run to k+4 and EN to k+2.
+  // Once every thread has finished compute_new(k), the OLD slots of planes up
+  // to k-1 and the EN slot of plane k are free, so OLD may run to k+DO-1 and
+  // EN to k+2.
   auto refill = [&](int k) {
     if (tid != PRODUCER) return;
-    while (old_next <= old_last && old_next <= k + 4) issue_old(old_next++);
-    if (!STAGE1)
+    while (old_next <= old_last && old_next <= k + DO - 1) issue_old(old_next++);
+    if (!STAGE1 && DE > 0)
       while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
   };
 
@@ -262,7 +277,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     return ok;
   };
   auto wait_en = [&]() {
-    if (STAGE1) return true;
+    if (STAGE1 || DE == 0) return true;
     const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1));
     ++ew;
     return ok;
@@ -275,8 +290,31 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const int gi = x0 - 1 + nxl, gj0 = y0 - 1 + CPT * nq;
   const bool out_x = gi < 0 || gi >= g.sx;
   const R* oth = old + (CPT * nq + 1) * OW + (nxl + 1);  // cell 0 in OLD slot 0; cell r at + r * OW
-  const R* enth = en + CPT * nq * OW + (nxl + 1);        // in EN slot 0
-  R* nwth = nw + CPT * nq * OW + nxl;                    // in NEW slot 0
+  const R* enth = en + CPT * nq * OW + (nxl + 1);        // in EN slot 0 (standard rings)
+  R* nwth = nw + CPT * nq * NP + nxl;                    // in NEW slot 0; cell r at + r * NP
+  // Lean rings: the step-start fields of this thread's cells, read from global
+  // memory into registers one plane ahead of use: compute_new(p) consumes
+  // plane p and then issues the loads of plane p+1, which the cleaning, the
+  // barrier and the next push hide
+  constexpr bool EN_REG = LEAN && !STAGE1;
+  bool en_ok[CPT];
+  long long ebase[CPT];
+  R en_nxt[CPT][6];
+#pragma unroll
+  for (int r = 0; r < CPT; ++r) {
+    const int gj = gj0 + r;
+    en_ok[r] = cell_thread && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
+    ebase[r] = en_ok[r] ? g.idx(gi, gj, 0) : 0;
+  }
+  auto en_load = [&](int p) {
+    if constexpr (EN_REG) {
+#pragma unroll
+      for (int r = 0; r < CPT; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+          en_nxt[r][c] = en_ok[r] ? __ldg(P.en_g[c] + ebase[r] + (long long)p * g.plane) : R(0);
+    }
+  };
   // B0 is read from global memory around the cell; cells of a partial tile
   // beyond the grid read around the nearest halo cell instead (their values
   // are computed but never used)
@@ -330,7 +368,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         const R f = a.b[1][c * S::OLDBOX];
-        const R fn = STAGE1 ? f : e1[c * S::ENBOX + r * OW];
+        R fn;
+        if constexpr (STAGE1) fn = f;
+        else if constexpr (EN_REG) fn = en_nxt[r][c];
+        else fn = e1[c * S::ENBOX + r * OW];
         w[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
       if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj0 + r, P.p.y0), p + P.p.z0, w);
@@ -414,7 +455,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 #pragma unroll
     for (int r = 0; r < CPT; ++r)
 #pragma unroll
-      for (int c = 0; c < 6; ++c) dst[r * OW + c * S::NEWPL] = v[r][c];
+      for (int c = 0; c < 6; ++c) dst[r * NP + c * S::NEWPL] = v[r][c];
+    en_load(p + 1);
   };
 
   // cleaned cells of this thread: (lx, CPT * lq + r) of the tile, tid < NCLEAN
@@ -434,7 +476,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     xy_images[r] = nxs > 1 || (per_y && (cj < NG || cj >= g.sy - NG));
     cbase[r] = c_in[r] ? g.idx(ci, cj, 0) : 0;
   }
-  const R* cth = nw + (CPT * lq + 1) * OW + (lx + 1);
+  const R* cth = nw + (CPT * lq + 1) * NP + (lx + 1);
 
   // clean plane k (m = k - kb: NEW slots of k-1, k, k+1 are m, m+1, m+2 mod 4)
   auto clean_store = [&](int k, int m) {
@@ -446,13 +488,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     R v[CPT][6];
 #pragma unroll
     for (int r = 0; r < CPT; ++r) {
-      SmemNew<R, TY> a;
-      a.b[0] = n0 + r * OW;
-      a.b[1] = n1 + r * OW;
-      a.b[2] = n2 + r * OW;
+      SmemNew<R, TY, LEAN> a;
+      a.b[0] = n0 + r * NP;
+      a.b[1] = n1 + r * NP;
+      a.b[2] = n2 + r * NP;
       R e[3];
       if constexpr (FD) clean_cell_fast(a, e, ct);
-      else clean_cell<R, C, SmemNew<R, TY>, false>(a, e, ct);
+      else clean_cell<R, C, SmemNew<R, TY, LEAN>, false>(a, e, ct);
       v[r][0] = e[0];
       v[r][1] = e[1];
       v[r][2] = e[2];
@@ -489,11 +531,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
   // `failed` is block-uniform: every wait result goes through a barrier-OR.
+  en_load(kb - 1);
   bool failed = __syncthreads_or(!(wait_old() & wait_old() & wait_old() & wait_en()));  // OLD kb-2..kb, EN kb-1
   if (!failed) {
     compute_new(kb - 1, 0, 0);
     failed = __syncthreads_or(!(wait_old() & wait_en()));  // OLD kb+1, EN kb
     if (!failed) {
+      refill(kb - 1);
       compute_new(kb, 1, 1);
       __syncthreads();
       // ---- march: one barrier per plane ------------------------------------
@@ -517,7 +561,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       // drain the copies that may still be in flight: the last use of each slot
       for (int p = max(kb - 2, old_next - DO); p < old_next; ++p)
         mbar_wait(bar_old + 8 * ((p - kb + 2) % DO), (unsigned)(((p - kb + 2) / DO) & 1));
-      if (!STAGE1)
+      if constexpr (!STAGE1 && DE > 0)
         for (int p = max(kb - 1, en_next - DE); p < en_next; ++p)
           mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1));
     }
@@ -535,9 +579,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 #if !defined(FFE_BATCH_TY)
 // One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).  Tile height 8.
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(Tile<8, fused_cpt<R>()>::NT, sizeof(R) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(Tile<8, fused_cpt<R>()>::NT, fused_lean<R>() ? 3 : 1)
     k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
-  stage_body<R, C, B0, ABS, STAGE1, 8, fused_cpt<R>()>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
+  stage_body<R, C, B0, ABS, STAGE1, 8, fused_cpt<R>(), fused_lean<R>()>(maps.in, maps.en, P, blockIdx.x, blockIdx.y,
+                                                                        blockIdx.z);
 }
 #else
 // Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
@@ -556,11 +601,11 @@ __global__ void __launch_bounds__(Tile<TY, fused_cpt<R>()>::NT, (sizeof(R) == 4 
     const BatchBox<R>& e = T.b[it.box];
     bool ok;
     if (e.has_b0) {
-      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, true, false, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, true, false, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     } else {
-      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, false, false, STAGE1, TY, fused_cpt<R>()>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else ok = stage_body<R, C, false, false, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     }
     if (!ok) return;
   }
@@ -797,7 +842,7 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   const int kz = fused_planes_per_block(g, TY);
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
-  const size_t smem = Sizes<R, TY>::BYTES;
+  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
   const bool abs = p.bnd[0] == 2;
   const bool s1 = stage == 1;
 #define FFE_GO(B0V, ABSV, S1V)                                                                   \
@@ -806,7 +851,9 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
     static bool attr_set = false;                                                                \
     if (!attr_set) {                                                                             \
       if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
-          cudaSuccess)                                                                           \
+              cudaSuccess ||                                                                     \
+          cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout,               \
+                               (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)              \
         return -3;                                                                               \
       attr_set = true;                                                                           \
     }                                                                                            \
