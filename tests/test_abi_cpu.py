@@ -85,3 +85,7 @@ def test_footprint_query_needs_no_gpu(lib):
     assert ffe.desc_device_bytes(psr) > ffe.desc_device_bytes(ffe.make_desc((64, 64, 64)))
     with pytest.raises(ffe.FFEError):
         ffe.desc_device_bytes(ffe.make_desc((1, 8, 8)))
+    # in-plane offsets of the fused kernels are 32-bit: planes of 2^31 elements are refused
+    assert ffe.desc_device_bytes(ffe.make_desc((46000, 46000, 2))) > 0
+    with pytest.raises(ffe.FFEError):
+        ffe.desc_device_bytes(ffe.make_desc((50000, 50000, 2)))

@@ -404,6 +404,7 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
         lr = launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi, me,
                                       ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
                                       ct, ubp, h->derr, h->st);
+      if (lr == -4) return fail(h, FFE_EINVAL, "fused stage: the arrays of a set are not equally spaced");
       if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
       if ((rc = check_launch(h, "fused stage"))) return rc;
       if (psr) {
@@ -527,6 +528,9 @@ int validate_desc(ffe_grid_desc& d) {
     return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
   for (int a = 0; a < 3; ++a)
     if (d.boundary[a] < 0 || d.boundary[a] > 2) return set_thread_err(FFE_EINVAL, "bad boundary %d", d.boundary[a]);
+  // the fused kernels hold in-plane offsets in 32 bits
+  if ((long long)(d.sx + 2 * FFE_NGHOST + 64) * (d.sy + 2 * FFE_NGHOST) >= (1LL << 31))
+    return set_thread_err(FFE_EINVAL, "a plane of more than 2^31 elements is not supported");
   // one absorbing axis makes all three absorbing (src/logistics/initialize.F90:144-148)
   if (d.boundary[0] == 2 || d.boundary[1] == 2 || d.boundary[2] == 2)
     d.boundary[0] = d.boundary[1] = d.boundary[2] = 2;
@@ -1218,11 +1222,10 @@ void fill_tables(ffe_batch* b, const std::vector<int>& cur0, const int32_t* step
           P.incr = incr ? 1 : 0;
           P.kz = b->kz_of[i];
           for (int k = 0; k < 3; ++k) P.b0[k] = (const R*)h->b0[k];
-          for (int k = 0; k < 6; ++k) {
-            P.in_g[k] = (const R*)h->set[ins[s]][k];
-            P.en_g[k] = (const R*)h->set[A][k];
-            P.out[k] = (R*)h->set[outs[s]][k];
-          }
+          P.in0 = (const R*)h->set[ins[s]][0];
+          P.en0 = (const R*)h->set[A][0];
+          P.out0 = (R*)h->set[outs[s]][0];
+          P.fs = (const R*)h->set[0][1] - (const R*)h->set[0][0];
           P.err = b->derr;
           P.ubc = uni ? 1 : 0;
           P.ub = ub;
@@ -1247,9 +1250,9 @@ void fill_tables(ffe_batch* b, const std::vector<int>& cur0, const int32_t* step
             psr_fix_box(h->g, q.i_lo, q.i_hi, q.j_lo, q.j_hi, q.k_lo, q.k_hi, u);
             F.ui = u[0]; F.uj = u[1]; F.uk = u[2]; F.ux = u[3]; F.uy = u[4]; F.uz = u[5];
             for (int k = 0; k < 6; ++k) {
-              F.in[k] = P.in_g[k];
-              F.en[k] = P.en_g[k];
-              F.out[k] = P.out[k];
+              F.in[k] = P.in0 + k * P.fs;
+              F.en[k] = P.en0 + k * P.fs;
+              F.out[k] = P.out0 + k * P.fs;
             }
             for (int k = 0; k < 3; ++k) F.b0[k] = P.b0[k];
             F.s1 = (R*)h->box;
@@ -1395,7 +1398,7 @@ int time_stage(ffe_batch* b, int reps, double* ms) {
     for (int l = 0; l < b->groups[gi].n; ++l) {
       BatchBox<R>& e = T->b[l];
       const int A = cur0[b->groups[gi].first + l];
-      for (int k = 0; k < 6; ++k) e.P.in_g[k] = (const R*)b->m[b->groups[gi].first + l]->set[A][k];
+      e.P.in0 = (const R*)b->m[b->groups[gi].first + l]->set[A][0];
       e.mi = e.me - 6;
     }
   }

@@ -220,9 +220,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
   const R cc = P.cc, c1 = P.c1, c2 = P.c2, c3 = P.c3, ct = P.ct;
   const bool incr = P.incr != 0;
-  R* out[6];
-#pragma unroll
-  for (int c = 0; c < 6; ++c) out[c] = P.out[c];
+  R* const out0 = P.out0;
+  const long long fs = P.fs;
 
   const unsigned bar_old = smem_u32(bars), bar_en = smem_u32(bars + DO);
 
@@ -298,21 +297,22 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // barrier and the next push hide
   constexpr bool EN_REG = LEAN && !STAGE1;
   bool en_ok[CPT];
-  long long ebase[CPT];
+  int ebase[CPT];  // in-plane offsets
   R en_nxt[CPT][6];
 #pragma unroll
   for (int r = 0; r < CPT; ++r) {
     const int gj = gj0 + r;
     en_ok[r] = cell_thread && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
-    ebase[r] = en_ok[r] ? g.idx(gi, gj, 0) : 0;
+    ebase[r] = en_ok[r] ? (gj + NG) * g.px + gi + g.ox : 0;
   }
   auto en_load = [&](int p) {
     if constexpr (EN_REG) {
 #pragma unroll
-      for (int r = 0; r < CPT; ++r)
+      for (int r = 0; r < CPT; ++r) {
+        const R* q = P.en0 + ((long long)(p + NG) * g.plane + ebase[r]);
 #pragma unroll
-        for (int c = 0; c < 6; ++c)
-          en_nxt[r][c] = en_ok[r] ? __ldg(P.en_g[c] + ebase[r] + (long long)p * g.plane) : R(0);
+        for (int c = 0; c < 6; ++c, q += fs) en_nxt[r][c] = en_ok[r] ? __ldg(q) : R(0);
+      }
     }
   };
   // B0 is read from global memory around the cell; cells of a partial tile
@@ -417,7 +417,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
                                  (!per_z && (wk == 0 || wk == g.sz - 1));
           if (near_open) {
             GlobalAcc<R> a;
-            for (int c = 0; c < 6; ++c) a.f[c] = P.in_g[c];
+            for (int c = 0; c < 6; ++c) a.f[c] = P.in0 + c * fs;
             a.b0 = P.b0;
             a.s = g.idx(wi, wj, wk);
             a.dj = g.px;
@@ -427,8 +427,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
             else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-              const R f = __ldg(P.in_g[c] + a.s);
-              const R fn = STAGE1 ? f : __ldg(P.en_g[c] + a.s);
+              const R f = __ldg(P.in0 + (c * fs + a.s));
+              const R fn = STAGE1 ? f : __ldg(P.en0 + (c * fs + a.s));
               v[r][c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
             }
             push = false;
@@ -468,13 +468,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   if (per_x && ci < NG) xs[nxs++] = ci + g.sx;
   if (per_x && ci >= g.sx - NG) xs[nxs++] = ci - g.sx;
   bool c_in[CPT], xy_images[CPT];
-  long long cbase[CPT];
+  int cbase[CPT];  // in-plane offsets
 #pragma unroll
   for (int r = 0; r < CPT; ++r) {
     const int cj = cj0 + r;
     c_in[r] = clean_thread && ci < g.sx && cj < g.sy;
     xy_images[r] = nxs > 1 || (per_y && (cj < NG || cj >= g.sy - NG));
-    cbase[r] = c_in[r] ? g.idx(ci, cj, 0) : 0;
+    cbase[r] = c_in[r] ? (cj + NG) * g.px + ci + g.ox : 0;
   }
   const R* cth = nw + (CPT * lq + 1) * NP + (lx + 1);
 
@@ -507,9 +507,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     for (int r = 0; r < CPT; ++r) {
       if (!c_in[r]) continue;
       if ((no_xy_images || !xy_images[r]) && !z_image) {
-        const long long o = cbase[r] + (long long)k * g.plane;
+        R* q = out0 + ((long long)(k + NG) * g.plane + cbase[r]);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) out[c][o] = v[r][c];
+        for (int c = 0; c < 6; ++c, q += fs) *q = v[r][c];
         continue;
       }
       const int cj = cj0 + r;
@@ -524,7 +524,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
           for (int a0 = 0; a0 < nxs; ++a0) {
             const long long o = g.idx(xs[a0], ys[a1], zs[a2]);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) out[c][o] = v[r][c];
+            for (int c = 0; c < 6; ++c) out0[o + c * fs] = v[r][c];
           }
     }
   };
@@ -796,7 +796,7 @@ __global__ void k_uniform_ghosts_batch(const FixItem* __restrict__ items, const 
   const int i = it.bx * 32 + (int)threadIdx.x - NG, j = it.by * 8 + (int)threadIdx.y - NG;
   if (i >= P.g.sx + NG || j >= P.g.sy + NG) return;
   const long long s = P.g.idx(i, j, it.bz);
-  uniform_bc_apply(P.ub, P.p, i, j, it.bz, P.out[0][s], P.out[1][s], P.out[5][s]);
+  uniform_bc_apply(P.ub, P.p, i, j, it.bz, P.out0[s], P.out0[s + P.fs], P.out0[s + 5 * P.fs]);
 }
 #endif
 
@@ -828,12 +828,14 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.c3 = c3;
   P.ct = ct;
   P.incr = incr ? 1 : 0;
-  for (int c = 0; c < 6; ++c) P.out[c] = out.c[c];
   for (int c = 0; c < 3; ++c) P.b0[c] = b0.c[c];
-  for (int c = 0; c < 6; ++c) {
-    P.in_g[c] = in_g.c[c];
-    P.en_g[c] = en_g.c[c];
-  }
+  // the kernel addresses component c as base + c * fs
+  P.in0 = in_g.c[0];
+  P.en0 = en_g.c[0];
+  P.out0 = out.c[0];
+  P.fs = out.c[1] - out.c[0];
+  for (int c = 0; c < 6; ++c)
+    if (in_g.c[c] != P.in0 + c * P.fs || en_g.c[c] != P.en0 + c * P.fs || out.c[c] != P.out0 + c * P.fs) return -4;
   P.err = err;
   P.ubc = ub ? 1 : 0;
   if (ub) P.ub = *ub;

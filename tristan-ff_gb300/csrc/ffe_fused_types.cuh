@@ -25,9 +25,12 @@ struct Params {
   int incr;
   int kz;  // planes per block
   const R* b0[3];
-  const R* in_g[6];  // stage input and step-start sets in global memory, for the
-  const R* en_g[6];  // few halo cells computed at their periodic image
-  R* out[6];
+  // The six arrays of a set lie at a fixed stride: component c of the stage
+  // input, step-start and output sets starts at in0, en0, out0 + c * fs.
+  const R* in0;
+  const R* en0;
+  R* out0;
+  long long fs;
   int* err;
   int ubc;  // apply the user_uniform BC inline (this step's constants in ub)
   UniformBC<R> ub;
