@@ -8,6 +8,7 @@ Translation units (compiled in parallel, then linked):
   csrc/ffe_fused.cu    fused stage kernels (fast: contraction on)
   csrc/ffe_fused.cu    again with -DFFE_FUSED_EXACT -fmad=false (verification path)
   csrc/ffe_fused.cu    with -DFFE_BATCH_TY=8 and =16: batched (many-grid) launches
+  csrc/ffe_fused.cu    with -DFFE_BATCH_TY=8 -DFFE_BATCH_SPEC: batched launches of one variant
   csrc/ffe_noalloc.cu  cleanEpar on caller-owned arrays, fixed device scratch
   csrc/ffe_output.cu   writeOutput's node datasets (interpolation + downsampling)
 Output: tristan-ff_gb300/lib/libffe_gb300.so (git-ignored; rebuilt on each box).
@@ -34,6 +35,7 @@ UNITS = [
     ("ffe_fused.cu", "ffe_fused_exact.o", ["-fmad=false", "-DFFE_FUSED_EXACT"]),
     ("ffe_fused.cu", "ffe_batch_t8.o", ["-DFFE_BATCH_TY=8"]),
     ("ffe_fused.cu", "ffe_batch_t16.o", ["-DFFE_BATCH_TY=16"]),
+    ("ffe_fused.cu", "ffe_batch_t8s.o", ["-DFFE_BATCH_TY=8", "-DFFE_BATCH_SPEC"]),
     ("ffe_noalloc.cu", "ffe_noalloc.o", ["-fmad=false"]),
     ("ffe_output.cu", "ffe_output.o", ["-fmad=false"]),
 ]

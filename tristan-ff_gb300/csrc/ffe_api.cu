@@ -1063,6 +1063,7 @@ struct ffe_batch {
   cudaEvent_t copied = nullptr;  // host staging of the fix-up table free again
   int ty = 8, kz = 0, persistent = 0;
   int blocks_per_sm = 0, sms = 0;
+  int spec_bps[4] = {0, 0, 0, 0};  // blocks per SM of the one-variant kernels (tile 8), 0: none
   int* derr = nullptr;           // device timeout word
   CUtensorMap* dmaps = nullptr;  // device: [tile 8|16][member][set][12 maps]
   std::vector<int> kz_of;        // planes per block of each member
@@ -1153,12 +1154,36 @@ template <typename R, int C> int prepare_kernels(int ty) {
     if (ty == 16) return fused_batch_prepare_t16<R, C>();
   return fused_batch_prepare_t8<R, C>();
 }
+// The B0 / absorbing-layer variant (bit 1 B0, bit 0 absorbing layer) shared
+// by the first n entries of a launch table, or -1 when they differ.
+template <typename R> int table_variant(const BoxTable<R>& T, int n) {
+  auto var = [&](int l) { return (T.b[l].has_b0 ? 2 : 0) | (T.b[l].absorb ? 1 : 0); };
+  const int v = n > 0 ? var(0) : -1;
+  for (int l = 1; l < n; ++l)
+    if (var(l) != v) return -1;
+  return v;
+}
+
+// One stage launch of a group: with tile height 8 and all entries of one
+// variant that has a specialised kernel, that kernel (the single-grid body);
+// otherwise the kernel that switches per grid.  Persistent launches size the
+// grid by the chosen kernel's residency.
 template <typename R, int C>
-int launch_batch_kernel(const ffe_batch* b, const ffe_batch::Group& gr, bool stage1, const BoxTable<R>& T,
-                        int grid) {
+int launch_batch_kernel(const ffe_batch* b, const ffe_batch::Group& gr, bool stage1, const BoxTable<R>& T) {
+  const int var = b->ty == 8 ? table_variant(T, gr.n) : -1;
+  const int bps = var >= 0 ? b->spec_bps[var] : 0;
+  auto grid_of = [&](int per_sm) {
+    return b->persistent ? std::max(1, std::min(gr.nitems, per_sm * b->sms)) : gr.nitems;
+  };
+  if (bps > 0) return launch_fused_batch_spec_t8<R, C>(stage1, var, gr.ditems, gr.nitems, T, grid_of(bps), b->st);
   if constexpr (sizeof(R) == 4)
-    if (b->ty == 16) return launch_fused_batch_t16<R, C>(stage1, gr.ditems, gr.nitems, T, grid, b->st);
-  return launch_fused_batch_t8<R, C>(stage1, gr.ditems, gr.nitems, T, grid, b->st);
+    if (b->ty == 16)
+      return launch_fused_batch_t16<R, C>(stage1, gr.ditems, gr.nitems, T, grid_of(b->blocks_per_sm), b->st);
+  return launch_fused_batch_t8<R, C>(stage1, gr.ditems, gr.nitems, T, grid_of(b->blocks_per_sm), b->st);
+}
+
+template <typename R, int C> void prepare_spec(ffe_batch* b) {
+  for (int v = 0; v < 4; ++v) b->spec_bps[v] = fused_batch_prepare_spec_t8<R, C>(v);
 }
 
 int prepare(ffe_batch* b) {
@@ -1168,12 +1193,10 @@ int prepare(ffe_batch* b) {
   else n = prepare_kernels<float, 0>(b->ty);
   if (n <= 0) return bfail(FFE_ECUDA, "batched stage kernel: cannot raise the shared-memory limit");
   b->blocks_per_sm = n;
+  if (b->precision == FFE_FP64) prepare_spec<double, 0>(b);
+  else if (b->precision == FFE_FP32C) prepare_spec<float, 1>(b);
+  else prepare_spec<float, 0>(b);
   return FFE_OK;
-}
-
-int launch_grid(const ffe_batch* b, const ffe_batch::Group& gr) {
-  if (!b->persistent) return gr.nitems;
-  return std::max(1, std::min(gr.nitems, b->blocks_per_sm * b->sms));
 }
 
 template <typename R> BoxTable<R>* host_table(ffe_batch* b, int n, int s, int gi) {
@@ -1273,7 +1296,7 @@ int launch_stage(ffe_batch* b, int n, int s) {
   for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
     const auto& gr = b->groups[gi];
     const BoxTable<R>& T = *host_table<R>(b, n, s, gi);
-    if (launch_batch_kernel<R, C>(b, gr, s == 0, T, launch_grid(b, gr))) return bfail(FFE_ECUDA, "batched stage launch");
+    if (launch_batch_kernel<R, C>(b, gr, s == 0, T)) return bfail(FFE_ECUDA, "batched stage launch");
     if (gr.nghost) launch_uniform_ghosts_batch<R>(gr.dghost, gr.nghost, T, b->st);
   }
   if (b->nfix)
@@ -1411,7 +1434,7 @@ int time_stage(ffe_batch* b, int reps, double* ms) {
     cudaEventRecord(t0, b->st);
     for (int gi = 0; gi < (int)b->groups.size(); ++gi) {
       const auto& gr = b->groups[gi];
-      bad |= launch_batch_kernel<R, C>(b, gr, false, *host_table<R>(b, 0, 1, gi), launch_grid(b, gr)) != 0;
+      bad |= launch_batch_kernel<R, C>(b, gr, false, *host_table<R>(b, 0, 1, gi)) != 0;
     }
     cudaEventRecord(t1, b->st);
     bad |= cudaEventSynchronize(t1) != cudaSuccess || cudaGetLastError() != cudaSuccess;

@@ -36,7 +36,9 @@
 // reciprocal-multiply quotient) as the fast path, and with -fmad=false under
 // FFE_FUSED_EXACT with correctly rounded division (bit-comparable with the
 // oracle).  Compiled a third and fourth time with -DFFE_BATCH_TY=8 / 16 for the
-// batched launches (many grids per launch, see k_fused_batch).
+// batched launches (many grids per launch, see k_fused_batch), and a fifth
+// time with -DFFE_BATCH_TY=8 -DFFE_BATCH_SPEC for the batched launches whose
+// grids all share one B0 / absorbing-layer variant (k_fused_batch_var).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cstring>
@@ -48,7 +50,11 @@
 #if defined(FFE_BATCH_TY)
 #define FFE_CAT2(a, b) a##b
 #define FFE_CAT(a, b) FFE_CAT2(a, b)
+#if defined(FFE_BATCH_SPEC)
+#define FFE_FUSED_NS FFE_CAT(FFE_CAT(fused_batch, FFE_BATCH_TY), s)
+#else
 #define FFE_FUSED_NS FFE_CAT(fused_batch, FFE_BATCH_TY)
+#endif
 #define FFE_FAST true
 #elif defined(FFE_FUSED_EXACT)
 #define FFE_FUSED_NS fused_exact
@@ -91,6 +97,9 @@ struct Tile {
 // for two blocks per SM at up to 168 registers; one in FP64
 template <typename R>
 constexpr int fused_cpt() { return sizeof(R) == 4 ? 2 : 1; }
+// the batched kernel inlines the four B0 / absorbing-layer variants of the
+// body; with one cell per thread it stays at two blocks per SM (TY = 8)
+constexpr int BATCH_CPT = 1;
 
 // Ring layout.  Standard (FP64, the batched kernels): OLD ring of 5 planes
 // (two planes of copies ahead of use), step-start fields in a 2-plane TMA
@@ -594,22 +603,43 @@ __global__ void __launch_bounds__(Tile<8, fused_cpt<R>()>::NT, fused_lean<R>() ?
 // block b takes items b, b + gridDim.x, ... (the host orders items by
 // decreasing work).
 template <typename R, int C, bool STAGE1, int TY>
-__global__ void __launch_bounds__(Tile<TY, fused_cpt<R>()>::NT, (sizeof(R) == 4 && TY == 8) ? 2 : 1)
+__global__ void __launch_bounds__(Tile<TY, BATCH_CPT>::NT, (sizeof(R) == 4 && TY == 8) ? 2 : 1)
     k_fused_batch(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const BatchItem it = items[w];
     const BatchBox<R>& e = T.b[it.box];
     bool ok;
     if (e.has_b0) {
-      if (e.absorb) ok = stage_body<R, C, true, true, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, true, false, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb)
+        ok = stage_body<R, C, true, true, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else
+        ok = stage_body<R, C, true, false, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     } else {
-      if (e.absorb) ok = stage_body<R, C, false, true, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
-      else ok = stage_body<R, C, false, false, STAGE1, TY, fused_cpt<R>(), false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      if (e.absorb)
+        ok = stage_body<R, C, false, true, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+      else
+        ok = stage_body<R, C, false, false, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     }
     if (!ok) return;
   }
 }
+
+#if defined(FFE_BATCH_SPEC)
+// Many grids of one variant (VAR: bit 1 B0, bit 0 absorbing layer) in one
+// launch: the body of the single-grid kernel (two cells per thread and lean
+// rings in FP32, three blocks per SM), items and table as in k_fused_batch.
+template <typename R, int C, bool STAGE1, int TY, int VAR>
+__global__ void __launch_bounds__(Tile<TY, fused_cpt<R>()>::NT, fused_lean<R>() ? 3 : 1)
+    k_fused_batch_var(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const BatchItem it = items[w];
+    const BatchBox<R>& e = T.b[it.box];
+    if (!stage_body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, STAGE1, TY, fused_cpt<R>(), fused_lean<R>()>(
+            e.mi, e.me, e.P, it.tx, it.ty, it.tz))
+      return;
+  }
+}
+#endif
 #endif
 
 // ---- rotating-conductor boundary condition on the fused path ---------------
@@ -985,6 +1015,68 @@ FFE_INST_X(float, 1)
 FFE_INST_X(float, 2)
 FFE_INST_X(double, 0)
 
+#elif defined(FFE_BATCH_SPEC)  // batched launches of one variant, tile height 8
+
+// One stage of many grids of variant var (0: plain, 3: B0 and absorbing
+// layer); -1 when var has no specialised kernel.  The shared-memory limit must
+// have been raised by fused_batch_prepare_spec_t8.
+template <typename R, int C>
+int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int nitems, const BoxTable<R>& T,
+                               int grid, cudaStream_t st) {
+  using namespace FFE_FUSED_NS;
+  constexpr int TY = FFE_BATCH_TY, NT = Tile<TY, fused_cpt<R>()>::NT;
+  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
+  if (nitems <= 0) return 0;
+  if (var == 0) {
+    if (stage1) k_fused_batch_var<R, C, true, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
+    else k_fused_batch_var<R, C, false, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
+  } else if (var == 3) {
+    if (stage1) k_fused_batch_var<R, C, true, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
+    else k_fused_batch_var<R, C, false, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+// Raise the shared-memory limit of the two stage kernels of variant var;
+// returns their resident blocks per SM, or 0 on failure.
+template <typename R, int C>
+int fused_batch_prepare_spec_t8(int var) {
+  using namespace FFE_FUSED_NS;
+  constexpr int TY = FFE_BATCH_TY, NT = Tile<TY, fused_cpt<R>()>::NT;
+  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
+  void (*k1)(const BatchItem*, int, const BoxTable<R>) = nullptr;
+  void (*k2)(const BatchItem*, int, const BoxTable<R>) = nullptr;
+  if (var == 0) {
+    k1 = k_fused_batch_var<R, C, true, TY, 0>;
+    k2 = k_fused_batch_var<R, C, false, TY, 0>;
+  } else if (var == 3) {
+    k1 = k_fused_batch_var<R, C, true, TY, 3>;
+    k2 = k_fused_batch_var<R, C, false, TY, 3>;
+  } else {
+    return 0;
+  }
+  int n[2] = {0, 0};
+  for (int i = 0; i < 2; ++i) {
+    const void* k = (const void*)(i ? k2 : k1);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n[i], k, NT, smem) != cudaSuccess)
+      return 0;
+  }
+  return n[0] < n[1] ? n[0] : n[1];
+}
+
+#define FFE_INST_S(R, C)                                                                                        \
+  template int launch_fused_batch_spec_t8<R, C>(bool, int, const BatchItem*, int, const BoxTable<R>&, int,     \
+                                                cudaStream_t);                                                  \
+  template int fused_batch_prepare_spec_t8<R, C>(int);
+FFE_INST_S(float, 0)
+FFE_INST_S(float, 1)
+FFE_INST_S(double, 0)
+
 #else  // FFE_BATCH_TY: batched launches for tile height FFE_BATCH_TY
 
 #define FFE_BATCH_LAUNCH FFE_CAT(launch_fused_batch_t, FFE_BATCH_TY)
@@ -1000,8 +1092,8 @@ int FFE_BATCH_LAUNCH(bool stage1, const BatchItem* items, int nitems, const BoxT
   constexpr int TY = FFE_BATCH_TY;
   const size_t smem = Sizes<R, TY>::BYTES;
   if (nitems <= 0) return 0;
-  if (stage1) k_fused_batch<R, C, true, TY><<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(items, nitems, T);
-  else k_fused_batch<R, C, false, TY><<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(items, nitems, T);
+  if (stage1) k_fused_batch<R, C, true, TY><<<grid, Tile<TY, BATCH_CPT>::NT, smem, st>>>(items, nitems, T);
+  else k_fused_batch<R, C, false, TY><<<grid, Tile<TY, BATCH_CPT>::NT, smem, st>>>(items, nitems, T);
   return 0;
 }
 
@@ -1017,8 +1109,8 @@ int FFE_BATCH_PREP() {
   if (cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   if (cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   int n1 = 0, n2 = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k1, Tile<TY, fused_cpt<R>()>::NT, smem) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k2, Tile<TY, fused_cpt<R>()>::NT, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k1, Tile<TY, BATCH_CPT>::NT, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k2, Tile<TY, BATCH_CPT>::NT, smem) != cudaSuccess) return 0;
   return n1 < n2 ? n1 : n2;
 }
 
