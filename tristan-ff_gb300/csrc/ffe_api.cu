@@ -662,7 +662,7 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
   h->maps_ok = true;
   for (int s = 0; s < 3 && h->maps_ok; ++s)
     for (int c = 0; c < 6 && h->maps_ok; ++c)
-      h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es, 8) == 0;
+      h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es, FUSED_TY) == 0;
   if (!h->maps_ok && d.path >= FFE_PATH_FUSED) {
     cudaFreeAsync(h->arena_raw, h->st);
     cudaStreamSynchronize(h->st);

@@ -95,25 +95,36 @@ struct Tile {
 };
 // cells per thread of the single-grid kernel: two in FP32, which leaves room
 // for two blocks per SM at up to 168 registers; one in FP64
-template <typename R>
-constexpr int fused_cpt() { return sizeof(R) == 4 ? 2 : 1; }
-// the batched kernel inlines the four B0 / absorbing-layer variants of the
-// body; with one cell per thread it stays at two blocks per SM (TY = 8)
+// The batched kernel that switches variants per grid inlines the four B0 /
+// absorbing-layer variants of the body; with one cell per thread it stays at
+// two blocks per SM (TY = 8).
 constexpr int BATCH_CPT = 1;
 
-// Ring layout.  Standard (FP64, the batched kernels): OLD ring of 5 planes
-// (two planes of copies ahead of use), step-start fields in a 2-plane TMA
-// ring, NEW rows of OW words.  Lean (the single-grid FP32 kernel): OLD ring of
-// 4 planes (one plane ahead), step-start fields loaded by each thread for its
-// own cells into registers one plane ahead, NEW rows of NX words: 74 KB of
-// shared memory at TY = 8, so that three blocks fit on an SM.
+// Ring layout.  Standard (FP64, the B0 and absorbing-layer variants, the
+// per-grid-switch batched kernel): OLD ring of 5 planes (two planes of copies
+// ahead of use), step-start fields in a 2-plane TMA ring.  Lean (the plain
+// FP32 variant): OLD ring of 4 planes (one plane ahead), step-start fields
+// loaded by each thread for its own cells into registers one plane ahead:
+// 74 KB of shared memory at TY = 8, so that three blocks fit on an SM.  NEW
+// rows are NX words in both.
 template <bool LEAN>
 struct Rings {
   static constexpr int DO = LEAN ? 4 : 5, DE = LEAN ? 0 : 2;
-  static constexpr int NP = LEAN ? NX : OW;  // NEW row pitch
+  static constexpr int NP = NX;  // NEW row pitch
 };
-template <typename R>
-constexpr bool fused_lean() { return sizeof(R) == 4; }
+
+// Configuration of the single-variant kernels (k_fused, k_fused_batch_var)
+// by element type and variant: the plain FP32 variant (no B0, no absorbing
+// layer) takes two cells per thread and lean rings at three blocks per SM (96
+// registers); the B0 and absorbing-layer variants, measured slower in that
+// form (a 160^3 pulsar stage: 321 us against 215 us), and FP64 take one cell
+// per thread and the standard rings (two blocks per SM in FP32, one in FP64).
+template <typename R, bool B0, bool ABS = false>
+struct Cfg {
+  static constexpr bool LEAN = sizeof(R) == 4 && !B0 && !ABS;
+  static constexpr int CPT = LEAN ? 2 : 1;
+  static constexpr int MINB = LEAN ? 3 : (sizeof(R) == 4 ? 2 : 1);
+};
 
 template <typename R, int TY, bool LEAN = false> struct Sizes {
   static constexpr int OLDBOX = ((OW * Tile<TY>::OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
@@ -586,12 +597,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 }
 
 #if !defined(FFE_BATCH_TY)
-// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk).  Tile height 8.
+// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk), tile height FUSED_TY.
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(Tile<8, fused_cpt<R>()>::NT, fused_lean<R>() ? 3 : 1)
+__global__ void __launch_bounds__(Tile<FUSED_TY, Cfg<R, B0, ABS>::CPT>::NT, Cfg<R, B0, ABS>::MINB)
     k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
-  stage_body<R, C, B0, ABS, STAGE1, 8, fused_cpt<R>(), fused_lean<R>()>(maps.in, maps.en, P, blockIdx.x, blockIdx.y,
-                                                                        blockIdx.z);
+  using CF = Cfg<R, B0, ABS>;
+  stage_body<R, C, B0, ABS, STAGE1, FUSED_TY, CF::CPT, CF::LEAN>(maps.in, maps.en, P, blockIdx.x, blockIdx.y,
+                                                                 blockIdx.z);
 }
 #else
 // Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
@@ -626,16 +638,18 @@ __global__ void __launch_bounds__(Tile<TY, BATCH_CPT>::NT, (sizeof(R) == 4 && TY
 
 #if defined(FFE_BATCH_SPEC)
 // Many grids of one variant (VAR: bit 1 B0, bit 0 absorbing layer) in one
-// launch: the body of the single-grid kernel (two cells per thread and lean
-// rings in FP32, three blocks per SM), items and table as in k_fused_batch.
+// launch: the body of the single-grid kernel in its configuration for that
+// variant (Cfg), items and table as in k_fused_batch.
 template <typename R, int C, bool STAGE1, int TY, int VAR>
-__global__ void __launch_bounds__(Tile<TY, fused_cpt<R>()>::NT, fused_lean<R>() ? 3 : 1)
+__global__ void __launch_bounds__(Tile<TY, Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>::CPT>::NT,
+                                  Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>::MINB)
     k_fused_batch_var(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
+  using CF = Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const BatchItem it = items[w];
     const BatchBox<R>& e = T.b[it.box];
-    if (!stage_body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, STAGE1, TY, fused_cpt<R>(), fused_lean<R>()>(
-            e.mi, e.me, e.P, it.tx, it.ty, it.tz))
+    if (!stage_body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, STAGE1, TY, CF::CPT, CF::LEAN>(e.mi, e.me, e.P, it.tx,
+                                                                                         it.ty, it.tz))
       return;
   }
 }
@@ -869,17 +883,17 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.err = err;
   P.ubc = ub ? 1 : 0;
   if (ub) P.ub = *ub;
-  constexpr int TY = 8;
+  constexpr int TY = FUSED_TY;
   const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
   const int kz = fused_planes_per_block(g, TY);
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
-  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
   const bool abs = p.bnd[0] == 2;
   const bool s1 = stage == 1;
 #define FFE_GO(B0V, ABSV, S1V)                                                                   \
   do {                                                                                           \
     auto kf = k_fused<R, C, B0V, ABSV, S1V>;                                                     \
+    const size_t smem = Sizes<R, TY, Cfg<R, B0V, ABSV>::LEAN>::BYTES;                            \
     static bool attr_set = false;                                                                \
     if (!attr_set) {                                                                             \
       if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
@@ -889,7 +903,7 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
         return -3;                                                                               \
       attr_set = true;                                                                           \
     }                                                                                            \
-    kf<<<grid, Tile<TY, fused_cpt<R>()>::NT, smem, st>>>(M, P);                                  \
+    kf<<<grid, Tile<TY, Cfg<R, B0V, ABSV>::CPT>::NT, smem, st>>>(M, P);                          \
   } while (0)
   if (has_b0) {
     if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
@@ -1017,20 +1031,28 @@ FFE_INST_X(double, 0)
 
 #elif defined(FFE_BATCH_SPEC)  // batched launches of one variant, tile height 8
 
-// One stage of many grids of variant var (0: plain, 3: B0 and absorbing
-// layer); -1 when var has no specialised kernel.  The shared-memory limit must
+// One stage of many grids of variant var (0: plain, 1: absorbing layer, 3:
+// B0 and absorbing layer); -1 when var has no specialised kernel.  The shared-memory limit must
 // have been raised by fused_batch_prepare_spec_t8.
 template <typename R, int C>
 int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int nitems, const BoxTable<R>& T,
                                int grid, cudaStream_t st) {
   using namespace FFE_FUSED_NS;
-  constexpr int TY = FFE_BATCH_TY, NT = Tile<TY, fused_cpt<R>()>::NT;
-  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
+  constexpr int TY = FFE_BATCH_TY;
   if (nitems <= 0) return 0;
   if (var == 0) {
+    constexpr int NT = Tile<TY, Cfg<R, false, false>::CPT>::NT;
+    const size_t smem = Sizes<R, TY, Cfg<R, false, false>::LEAN>::BYTES;
     if (stage1) k_fused_batch_var<R, C, true, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
+  } else if (var == 1) {
+    constexpr int NT = Tile<TY, Cfg<R, false, true>::CPT>::NT;
+    const size_t smem = Sizes<R, TY, Cfg<R, false, true>::LEAN>::BYTES;
+    if (stage1) k_fused_batch_var<R, C, true, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
+    else k_fused_batch_var<R, C, false, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
   } else if (var == 3) {
+    constexpr int NT = Tile<TY, Cfg<R, true, true>::CPT>::NT;
+    const size_t smem = Sizes<R, TY, Cfg<R, true, true>::LEAN>::BYTES;
     if (stage1) k_fused_batch_var<R, C, true, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
   } else {
@@ -1044,13 +1066,19 @@ int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int
 template <typename R, int C>
 int fused_batch_prepare_spec_t8(int var) {
   using namespace FFE_FUSED_NS;
-  constexpr int TY = FFE_BATCH_TY, NT = Tile<TY, fused_cpt<R>()>::NT;
-  const size_t smem = Sizes<R, TY, fused_lean<R>()>::BYTES;
+  constexpr int TY = FFE_BATCH_TY;
+  // only the plain variant takes the lean rings (Cfg)
+  const int NT = var == 0 ? Tile<TY, Cfg<R, false, false>::CPT>::NT : Tile<TY, Cfg<R, true, true>::CPT>::NT;
+  const size_t smem =
+      var == 0 ? Sizes<R, TY, Cfg<R, false, false>::LEAN>::BYTES : Sizes<R, TY, Cfg<R, true, true>::LEAN>::BYTES;
   void (*k1)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   void (*k2)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   if (var == 0) {
     k1 = k_fused_batch_var<R, C, true, TY, 0>;
     k2 = k_fused_batch_var<R, C, false, TY, 0>;
+  } else if (var == 1) {
+    k1 = k_fused_batch_var<R, C, true, TY, 1>;
+    k2 = k_fused_batch_var<R, C, false, TY, 1>;
   } else if (var == 3) {
     k1 = k_fused_batch_var<R, C, true, TY, 3>;
     k2 = k_fused_batch_var<R, C, false, TY, 3>;

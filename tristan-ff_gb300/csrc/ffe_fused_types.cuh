@@ -9,6 +9,7 @@ namespace ffe {
 // Tile of the fused stage kernel: TX x TY cells per block, TX fixed at one warp
 // width.  The tile height TY is a template parameter (8 or 16).
 constexpr int FUSED_TX = 32;
+constexpr int FUSED_TY = 8;  // tile height of the single-grid stage kernel
 
 struct Maps {  // one 3-D tensor map per component: stage input (OLD) and step start (EN)
   CUtensorMap in[6];
