@@ -238,6 +238,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const int ke = min(kb + P.kz, g.sz);
   const bool per_x = P.p.bnd[0] == 1, per_y = P.p.bnd[1] == 1, per_z = P.p.bnd[2] == 1;
   constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  // fast-path sums as row-grouped trees in the plain variant (whatever the
+  // kernel), in the reference's order in the B0 and absorbing-layer variants
+  constexpr bool TREE = !B0 && !ABS;
   const R cc = P.cc, c1 = P.c1, c2 = P.c2, c3 = P.c3, ct = P.ct;
   const bool incr = P.incr != 0;
   R* const out0 = P.out0;
@@ -383,7 +386,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       a.dj = g.px;
       a.dk = g.plane;
       R d[6];
-      if constexpr (FD) push_cell_fast<B0>(a, cc, d);
+      if constexpr (FD) push_cell_fast<B0, TREE>(a, cc, d);
       else push_cell<R, C, B0, SmemOld<R, TY>, false>(a, cc, d);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
@@ -443,7 +446,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
             a.dj = g.px;
             a.dk = g.plane;
             R d[6];
-            if constexpr (FD) push_cell_fast<B0>(a, cc, d);
+            if constexpr (FD) push_cell_fast<B0, TREE>(a, cc, d);
             else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
@@ -513,7 +516,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       a.b[1] = n1 + r * NP;
       a.b[2] = n2 + r * NP;
       R e[3];
-      if constexpr (FD) clean_cell_fast(a, e, ct);
+      if constexpr (FD) clean_cell_fast<TREE>(a, e, ct);
       else clean_cell<R, C, SmemNew<R, TY, LEAN>, false>(a, e, ct);
       v[r][0] = e[0];
       v[r][1] = e[1];
@@ -715,7 +718,7 @@ __device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, i
     a.dj = g.px;
     a.dk = g.plane;
     R d[6];
-    if constexpr (FD) push_cell_fast<B0>(a, F.cc, d);
+    if constexpr (FD) push_cell_fast<B0, false>(a, F.cc, d);  // the reference's order of the sums
     else push_cell<R, C, B0, GlobalAcc<R>, false>(a, F.cc, d);
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -776,7 +779,7 @@ __device__ __forceinline__ void fix_clean_cell(const FixParams<R>& F, int bi, in
   a.dj = F.ux;
   a.dk = (long long)F.ux * F.uy;
   R e[3];
-  if constexpr (FD) clean_cell_fast(a, e, F.ct);
+  if constexpr (FD) clean_cell_fast<false>(a, e, F.ct);
   else clean_cell<R, C, BoxAcc<R>, false>(a, e, F.ct);
   const long long s = g.idx(i, j, k);
   F.out[0][s] = e[0];

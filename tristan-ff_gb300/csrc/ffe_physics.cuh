@@ -220,12 +220,13 @@ __device__ __forceinline__ void clean_cell(const A& a, R e[3], R ct = R(0)) {
 //   64 B^2 = S8^2 + 16 (S2a^2 + S2b^2),   64 E^2 = 64 e0^2 + 4 (S4a^2 + S4b^2),
 //   J_i    = 4 CC / (64 B^2 + 64 TINY) * Srho * (cross product of bare sums),
 //   clean:   E_i -= (S.B-sums dot) * S8 / (64 B^2 + 64 ct).
-// The four- and eight-term sums are added as balanced trees (dependency depth
-// 2 and 3 instead of 3 and 7) grouped by y row: the sub-sum of one row is the
-// same expression for the two cells that share the row when a thread updates
-// two cells stacked in y, so it is evaluated once.  Unlike the exact path this
+// With TREE the four- and eight-term sums are added as balanced trees
+// (dependency depth 2 and 3 instead of 3 and 7) grouped by y row: the sub-sum
+// of one row is the same expression for the two cells that share the row when
+// a thread updates two cells stacked in y, so it is evaluated once.  This
 // changes the association of the reference's sums (rounding differences of
-// an ulp or so per average).
+// an ulp or so per average).  Without TREE the sums keep the reference's
+// left-to-right order (fewer live registers for one cell per thread).
 // ---------------------------------------------------------------------------
 // The hardware square-root approximation (PTX sqrt.approx.f32; +0 -> +0),
 // for the limiter's ratio in the fast path.
@@ -265,20 +266,41 @@ __device__ __forceinline__ float oct(const A& a, int c, int dx, int dy, int dz) 
 struct PointSums {
   float sa, sb, s8, s2a, s2b;
 };
-template <class A>
+template <bool TREE, class A>
 __device__ __forceinline__ PointSums sums_x(const A& a) {  // Ex point: Ey, Ez; Bx; By, Bz
-  return {xpair(a, EY, 1, 0, 0) + xpair(a, EY, 1, -1, 0), xpair(a, EZ, 1, 0, 0) + xpair(a, EZ, 1, 0, -1),
-          oct(a, BX, 1, -1, -1), a(BY, 0, 0, 0) + a(BY, 0, 0, -1), a(BZ, 0, 0, 0) + a(BZ, 0, -1, 0)};
+  const float s2a = a(BY, 0, 0, 0) + a(BY, 0, 0, -1), s2b = a(BZ, 0, 0, 0) + a(BZ, 0, -1, 0);
+  if constexpr (TREE)
+    return {xpair(a, EY, 1, 0, 0) + xpair(a, EY, 1, -1, 0), xpair(a, EZ, 1, 0, 0) + xpair(a, EZ, 1, 0, -1),
+            oct(a, BX, 1, -1, -1), s2a, s2b};
+  return {((a(EY, 0, 0, 0) + a(EY, 1, 0, 0)) + a(EY, 0, -1, 0)) + a(EY, 1, -1, 0),
+          ((a(EZ, 0, 0, 0) + a(EZ, 1, 0, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 1, 0, -1),
+          ((((((a(BX, 0, 0, 0) + a(BX, 0, -1, 0)) + a(BX, 1, -1, 0)) + a(BX, 1, 0, 0)) + a(BX, 0, 0, -1)) +
+            a(BX, 0, -1, -1)) + a(BX, 1, -1, -1)) + a(BX, 1, 0, -1),
+          s2a, s2b};
 }
-template <class A>
+template <bool TREE, class A>
 __device__ __forceinline__ PointSums sums_y(const A& a) {  // Ey point: Ex, Ez; By; Bx, Bz
-  return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 1, 0), zpair(a, EZ, 0, -1) + zpair(a, EZ, 1, -1),
-          oct(a, BY, -1, 1, -1), a(BX, 0, 0, 0) + a(BX, 0, 0, -1), a(BZ, 0, 0, 0) + a(BZ, -1, 0, 0)};
+  const float s2a = a(BX, 0, 0, 0) + a(BX, 0, 0, -1), s2b = a(BZ, 0, 0, 0) + a(BZ, -1, 0, 0);
+  if constexpr (TREE)
+    return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 1, 0), zpair(a, EZ, 0, -1) + zpair(a, EZ, 1, -1),
+            oct(a, BY, -1, 1, -1), s2a, s2b};
+  return {((a(EX, 0, 0, 0) + a(EX, -1, 0, 0)) + a(EX, 0, 1, 0)) + a(EX, -1, 1, 0),
+          ((a(EZ, 0, 0, 0) + a(EZ, 0, 1, 0)) + a(EZ, 0, 0, -1)) + a(EZ, 0, 1, -1),
+          ((((((a(BY, 0, 0, 0) + a(BY, -1, 0, 0)) + a(BY, -1, 1, 0)) + a(BY, 0, 1, 0)) + a(BY, 0, 0, -1)) +
+            a(BY, -1, 0, -1)) + a(BY, -1, 1, -1)) + a(BY, 0, 1, -1),
+          s2a, s2b};
 }
-template <class A>
+template <bool TREE, class A>
 __device__ __forceinline__ PointSums sums_z(const A& a) {  // Ez point: Ex, Ey; Bz; Bx, By
-  return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 0, 1), zpair(a, EY, 0, 1) + zpair(a, EY, -1, 1),
-          oct(a, BZ, -1, -1, 1), a(BX, 0, 0, 0) + a(BX, 0, -1, 0), a(BY, 0, 0, 0) + a(BY, -1, 0, 0)};
+  const float s2a = a(BX, 0, 0, 0) + a(BX, 0, -1, 0), s2b = a(BY, 0, 0, 0) + a(BY, -1, 0, 0);
+  if constexpr (TREE)
+    return {xpair(a, EX, -1, 0, 0) + xpair(a, EX, -1, 0, 1), zpair(a, EY, 0, 1) + zpair(a, EY, -1, 1),
+            oct(a, BZ, -1, -1, 1), s2a, s2b};
+  return {((a(EX, 0, 0, 0) + a(EX, -1, 0, 0)) + a(EX, 0, 0, 1)) + a(EX, -1, 0, 1),
+          ((a(EY, 0, 0, 0) + a(EY, 0, -1, 0)) + a(EY, 0, 0, 1)) + a(EY, 0, -1, 1),
+          ((((((a(BZ, 0, 0, 0) + a(BZ, -1, 0, 0)) + a(BZ, -1, -1, 0)) + a(BZ, 0, -1, 0)) + a(BZ, 0, 0, 1)) +
+            a(BZ, -1, 0, 1)) + a(BZ, -1, -1, 1)) + a(BZ, 0, -1, 1),
+          s2a, s2b};
 }
 
 __device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, const PointSums& s,
@@ -292,7 +314,7 @@ __device__ __forceinline__ float fast_current(float cc4, float t64, float sr, fl
   return __fdividef(cc4, bm + t64) * sr;
 }
 
-template <bool B0, class A>
+template <bool B0, bool TREE, class A>
 __device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6]) {
   const float ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const float bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -311,40 +333,40 @@ __device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6])
   const float cc4 = 4.f * cc, t64 = 64.f * tiny<float>();
   float ea, eb, k;
   {  // X current at the Ex point (field_solver.F90:91-111)
-    const PointSums s = sums_x(a);
+    const PointSums s = sums_x<TREE>(a);
     k = fast_current(cc4, t64, a.rho(1, 0, 0) + r0, ex0, s, ea, eb);
     d[0] = -(cc * cbx) - k * (ea * s.s2b - s.s2a * eb);
   }
   {  // Y current at the Ey point (:114-134)
-    const PointSums s = sums_y(a);
+    const PointSums s = sums_y<TREE>(a);
     k = fast_current(cc4, t64, a.rho(0, 1, 0) + r0, ey0, s, ea, eb);
     d[1] = -(cc * cby) - k * (eb * s.s2a - ea * s.s2b);
   }
   {  // Z current at the Ez point (:137-157)
-    const PointSums s = sums_z(a);
+    const PointSums s = sums_z<TREE>(a);
     k = fast_current(cc4, t64, r0 + a.rho(0, 0, 1), ez0, s, ea, eb);
     d[2] = -(cc * cbz) - k * (ea * s.s2b - s.s2a * eb);
   }
 }
 
-template <class A>
+template <bool TREE, class A>
 __device__ __forceinline__ void clean_cell_fast(const A& a, float e[3], float ct) {
   const float ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const float c64 = 64.f * ct;
   {  // Ex point (:289-300)
-    const PointSums s = sums_x(a);
+    const PointSums s = sums_x<TREE>(a);
     const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = ex0 * s.s8 + s.sa * s.s2a + s.sb * s.s2b;
     e[0] = ex0 - __fdividef(ep * s.s8, bm + c64);
   }
   {  // Ey point (:303-314)
-    const PointSums s = sums_y(a);
+    const PointSums s = sums_y<TREE>(a);
     const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = s.sa * s.s2a + ey0 * s.s8 + s.sb * s.s2b;
     e[1] = ey0 - __fdividef(ep * s.s8, bm + c64);
   }
   {  // Ez point (:317-328)
-    const PointSums s = sums_z(a);
+    const PointSums s = sums_z<TREE>(a);
     const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = s.sa * s.s2a + s.sb * s.s2b + ez0 * s.s8;
     e[2] = ez0 - __fdividef(ep * s.s8, bm + c64);
