@@ -61,6 +61,10 @@ def parse():
                          "one grid at a time; serve: a Poisson stream of pulsar runs, continuous batching "
                          "vs one grid at a time")
     ap.add_argument("--batch-boxes", type=int, default=64)
+    ap.add_argument("--batch-kind", default="mixed", choices=["mixed", "packet"],
+                    help="batch: half packets and half flux tubes (which carry a B0 field), or packets only")
+    ap.add_argument("--tile-y", type=int, default=0, choices=[0, 8, 16],
+                    help="batch: fixed tile height instead of the autotuned tiling (0: autotune)")
     ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
     ap.add_argument("--budget-gb", type=float, default=180.0, help="serve: HBM admission budget")
     ap.add_argument("--epoch-steps", type=int, default=32, help="serve: steps per batched epoch at most")
@@ -334,7 +338,7 @@ def bench_batch(args):
     torch.cuda.set_device(0)
     ffe_build.build()
     prec = ffe.PRECISIONS[args.precision]
-    specs = workloads.batch_boxes(args.batch_boxes)
+    specs = workloads.batch_boxes(args.batch_boxes, kind=args.batch_kind)
     cells = [s["size"][0] * s["size"][1] * s["size"][2] for s in specs]
     K = args.steps
     # one grid at a time: each box runs all K steps, then the next box
@@ -355,7 +359,11 @@ def bench_batch(args):
     b = ffe.Batch(bat)
     b.step(args.warmup)
     b.synchronize()
-    tune_ms = b.autotune(reps=3)
+    if args.tile_y:
+        b.set_tiling(args.tile_y, 0, False)
+        tune_ms = None
+    else:
+        tune_ms = b.autotune(reps=3)
     tiling = b.tiling()
     t0 = time.perf_counter()
     b.step(K, step0=[args.warmup] * len(bat))
@@ -382,8 +390,10 @@ def bench_batch(args):
                              "one_at_a_time": {"p50": pct(done, 50), "p99": pct(done, 99)}},
         "max_rel_l2_batched_vs_single": diff, "tiling": tiling, "autotune_ms_per_stage": tune_ms,
         "gpu_launches": launches * K,
-        "config": {"workload": "%d boxes, sides U[48,160], half Alfven packets, half twisted flux tubes"
-                               % len(specs), "cells": int(sum(cells)),
+        "config": {"workload": "%d boxes, sides U[48,160], %s"
+                               % (len(specs), "Alfven packets" if args.batch_kind == "packet"
+                                  else "half Alfven packets, half twisted flux tubes"),
+                   "cells": int(sum(cells)),
                    "timing": "host clock around synchronised runs (includes launch overhead of both paths)"},
     }))
 

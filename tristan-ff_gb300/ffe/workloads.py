@@ -108,15 +108,16 @@ def psr_params(side, incl_deg, cc=0.45):
     return (radius, float(incl_deg), period, 1.0)
 
 
-def batch_boxes(n=64, seed=3, lo=48, hi=160):
+def batch_boxes(n=64, seed=3, lo=48, hi=160, kind="mixed"):
     """The batched workload: n boxes with sides uniform in [lo, hi] per axis;
     the first half Alfven packets (periodic), the rest twisted flux tubes
-    (periodic x, y; open z) with twist amplitude U[0.1, 0.5]."""
+    (periodic x, y; open z) with twist amplitude U[0.1, 0.5].  kind="packet":
+    all Alfven packets."""
     rng = np.random.Generator(np.random.PCG64(seed))
     specs = []
     for b in range(n):
         size = tuple(int(v) for v in rng.integers(lo, hi + 1, size=3))
-        if b < n // 2:
+        if b < n // 2 or kind == "packet":
             specs.append({"kind": "packet", "size": size, "seed": int(rng.integers(1 << 30))})
         else:
             specs.append({"kind": "tube", "size": size, "beta": float(rng.uniform(0.1, 0.5))})
