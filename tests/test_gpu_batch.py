@@ -85,6 +85,33 @@ def test_batch_matches_single_grid_fused_path(prec):
     close(b_)
 
 
+@pytest.mark.parametrize("prec", [ffe.FP32, ffe.FP32C])
+@pytest.mark.parametrize("kind", ["packet", "psr"])
+def test_one_variant_batch_equals_single_grid_bit_for_bit(kind, prec):
+    """A batch whose grids all have one variant (plain packets; pulsars with
+    the absorbing layer) runs the single-grid kernel body at tile height 8:
+    every member equals its own single-grid run bit for bit."""
+    if kind == "packet":
+        specs = [{"kind": "packet", "size": (37, 24, 30), "seed": 5},
+                 {"kind": "packet", "size": (64, 17, 9), "seed": 6},
+                 {"kind": "packet", "size": (70, 41, 19), "seed": 7}]
+    else:
+        specs = [{"kind": "psr", "size": (44, 44, 44), "incl": 30.0, "absorb_buff": 5, "shell": "true_y"},
+                 {"kind": "psr", "size": (52, 40, 36), "incl": 60.0, "absorb_buff": 5, "shell": "true_y"}]
+    a, b_ = make(specs, prec), make(specs, prec)
+    s0 = [0, 3, 7][:len(specs)]
+    with ffe.Batch(a) as b:
+        b.set_tiling(8, 0, False)
+        b.step(4, step0=s0)
+        b.synchronize()
+    for s, k0 in zip(b_, s0):
+        s.mainloop(4, k0)
+        s.synchronize()
+    assert_equal_fields(fields(a), fields(b_))
+    close(a)
+    close(b_)
+
+
 def test_batch_fp64_matches_oracle(oracle_mod):
     """Three members (one per setup) from the same initial state: the batch on
     the GPU, each member alone in the oracle."""
