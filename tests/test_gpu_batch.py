@@ -194,7 +194,9 @@ def test_more_members_than_one_launch_holds():
                      {"kind": "tube", "size": size, "beta": 0.1 + 0.005 * i})
     mix = make(specs, ffe.FP32)
     with ffe.Batch(mix) as b:
-        assert b.launches() == 3 * (2 + 2)  # 2 groups, each with tube ghost planes
+        # 2 groups, each with one stage launch per variant (plain packets, tubes
+        # with B0) and one of the tubes' ghost planes
+        assert b.launches() == 3 * (2 * 2 + 2)
         b.step(3)
         b.synchronize()
     got = fields(mix)

@@ -1048,6 +1048,11 @@ struct ffe_batch {
     int nitems = 0, cap = 0;
     FixItem* dghost = nullptr;     // user_uniform ghost-plane items (box = index in the group)
     int nghost = 0;
+    // B0 / absorbing-layer variant of each member when the items were built
+    // (bit 1 B0, bit 0 absorbing layer); the items are ordered by variant,
+    // those of variant v at [vfirst[v], vfirst[v] + vcount[v])
+    int mvar[BATCH_MAX] = {};
+    int vfirst[4] = {}, vcount[4] = {};
   };
   struct G {
     int steps;
@@ -1109,8 +1114,11 @@ void drop_graphs(ffe_batch* b) {
 
 int tile_index(int ty) { return ty == 16 ? 1 : 0; }
 
-// Work items of the current tiling per group, largest blocks first (the
-// hardware and the persistent loop both take items in order).
+int variant_of(const ffe_solver* h) { return (h->has_b0 ? 2 : 0) | (h->p.bnd[0] == 2 ? 1 : 0); }
+
+// Work items of the current tiling per group, by variant and within a
+// variant largest blocks first (the hardware and the persistent loop both
+// take items in order).
 int build_items(ffe_batch* b) {
   const int nm = (int)b->m.size();
   b->kz_of.assign(nm, 0);
@@ -1118,6 +1126,7 @@ int build_items(ffe_batch* b) {
     std::vector<std::pair<long long, BatchItem>> it;
     for (int l = 0; l < gr.n; ++l) {
       const int i = gr.first + l;
+      gr.mvar[l] = variant_of(b->m[i]);
       const Geom& g = b->m[i]->g;
       const int kz = b->kz ? std::min(b->kz, g.sz) : fused_planes_per_block(g, b->ty);
       b->kz_of[i] = kz;
@@ -1130,9 +1139,17 @@ int build_items(ffe_batch* b) {
             it.push_back({w, BatchItem{l, x, y, z}});
           }
     }
-    std::stable_sort(it.begin(), it.end(), [](const auto& a, const auto& c) { return a.first > c.first; });
+    std::stable_sort(it.begin(), it.end(), [&](const auto& a, const auto& c) {
+      const int va = gr.mvar[a.second.box], vc = gr.mvar[c.second.box];
+      return va != vc ? va < vc : a.first > c.first;
+    });
     std::vector<BatchItem> v(it.size());
-    for (size_t k = 0; k < it.size(); ++k) v[k] = it[k].second;
+    for (int q = 0; q < 4; ++q) gr.vfirst[q] = gr.vcount[q] = 0;
+    for (size_t k = 0; k < it.size(); ++k) {
+      v[k] = it[k].second;
+      const int q = gr.mvar[v[k].box];
+      if (gr.vcount[q]++ == 0) gr.vfirst[q] = (int)k;
+    }
     if ((int)v.size() > gr.cap) {
       if (gr.ditems) cudaFree(gr.ditems);
       gr.ditems = nullptr;
@@ -1154,32 +1171,40 @@ template <typename R, int C> int prepare_kernels(int ty) {
     if (ty == 16) return fused_batch_prepare_t16<R, C>();
   return fused_batch_prepare_t8<R, C>();
 }
-// The B0 / absorbing-layer variant (bit 1 B0, bit 0 absorbing layer) shared
-// by the first n entries of a launch table, or -1 when they differ.
-template <typename R> int table_variant(const BoxTable<R>& T, int n) {
-  auto var = [&](int l) { return (T.b[l].has_b0 ? 2 : 0) | (T.b[l].absorb ? 1 : 0); };
-  const int v = n > 0 ? var(0) : -1;
-  for (int l = 1; l < n; ++l)
-    if (var(l) != v) return -1;
-  return v;
+// True when every entry of the launch table still has the variant its items
+// were built with (a member's B0 may have been set since).
+template <typename R> bool variants_current(const ffe_batch::Group& gr, const BoxTable<R>& T) {
+  for (int l = 0; l < gr.n; ++l)
+    if (((T.b[l].has_b0 ? 2 : 0) | (T.b[l].absorb ? 1 : 0)) != gr.mvar[l]) return false;
+  return true;
 }
 
-// One stage launch of a group: with tile height 8 and all entries of one
-// variant that has a specialised kernel, that kernel (the single-grid body);
-// otherwise the kernel that switches per grid.  Persistent launches size the
-// grid by the chosen kernel's residency.
+// Stage launches of a group: with tile height 8, one launch per variant
+// present, each of a specialised kernel (the single-grid body of that
+// variant) over the items of its variant; with tile height 16, or when a
+// member's variant changed since the items were built, one launch of the
+// kernel that switches per grid.  Persistent launches size the grid by the
+// chosen kernel's residency.
 template <typename R, int C>
 int launch_batch_kernel(const ffe_batch* b, const ffe_batch::Group& gr, bool stage1, const BoxTable<R>& T) {
-  const int var = b->ty == 8 ? table_variant(T, gr.n) : -1;
-  const int bps = var >= 0 ? b->spec_bps[var] : 0;
-  auto grid_of = [&](int per_sm) {
-    return b->persistent ? std::max(1, std::min(gr.nitems, per_sm * b->sms)) : gr.nitems;
+  auto grid_of = [&](int n, int per_sm) { return b->persistent ? std::max(1, std::min(n, per_sm * b->sms)) : n; };
+  auto generic = [&](const BatchItem* it, int n) -> int {
+    if (n <= 0) return 0;
+    if constexpr (sizeof(R) == 4)
+      if (b->ty == 16) return launch_fused_batch_t16<R, C>(stage1, it, n, T, grid_of(n, b->blocks_per_sm), b->st);
+    return launch_fused_batch_t8<R, C>(stage1, it, n, T, grid_of(n, b->blocks_per_sm), b->st);
   };
-  if (bps > 0) return launch_fused_batch_spec_t8<R, C>(stage1, var, gr.ditems, gr.nitems, T, grid_of(bps), b->st);
-  if constexpr (sizeof(R) == 4)
-    if (b->ty == 16)
-      return launch_fused_batch_t16<R, C>(stage1, gr.ditems, gr.nitems, T, grid_of(b->blocks_per_sm), b->st);
-  return launch_fused_batch_t8<R, C>(stage1, gr.ditems, gr.nitems, T, grid_of(b->blocks_per_sm), b->st);
+  if (b->ty != 8 || !variants_current(gr, T)) return generic(gr.ditems, gr.nitems);
+  for (int v = 0; v < 4; ++v) {
+    const int n = gr.vcount[v];
+    if (n <= 0) continue;
+    const BatchItem* it = gr.ditems + gr.vfirst[v];
+    const int rc = b->spec_bps[v] > 0
+                       ? launch_fused_batch_spec_t8<R, C>(stage1, v, it, n, T, grid_of(n, b->spec_bps[v]), b->st)
+                       : generic(it, n);
+    if (rc) return rc;
+  }
+  return 0;
 }
 
 template <typename R, int C> void prepare_spec(ffe_batch* b) {
@@ -1665,9 +1690,14 @@ int ffe_batch_autotune(ffe_batch_t b, int32_t reps, double* best_ms) {
 
 int ffe_batch_launches(ffe_batch_t b, int32_t* per_step) {
   if (!b || !per_step) return bfail(FFE_EINVAL, "null argument");
-  int ng = 0;
-  for (auto& gr : b->groups) ng += gr.nghost ? 1 : 0;
-  *per_step = 3 * ((int)b->groups.size() + ng + (b->nfix ? 3 : 0));
+  int ng = 0, ns = 0;
+  for (auto& gr : b->groups) {
+    ng += gr.nghost ? 1 : 0;
+    int nv = 0;  // stage launches of the group: one per variant present at tile height 8
+    for (int v = 0; v < 4; ++v) nv += gr.vcount[v] > 0 ? 1 : 0;
+    ns += b->ty == 8 && nv > 0 ? nv : 1;
+  }
+  *per_step = 3 * (ns + ng + (b->nfix ? 3 : 0));
   return FFE_OK;
 }
 

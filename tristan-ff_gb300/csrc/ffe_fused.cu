@@ -1034,8 +1034,8 @@ FFE_INST_X(double, 0)
 
 #elif defined(FFE_BATCH_SPEC)  // batched launches of one variant, tile height 8
 
-// One stage of many grids of variant var (0: plain, 1: absorbing layer, 3:
-// B0 and absorbing layer); -1 when var has no specialised kernel.  The shared-memory limit must
+// One stage of many grids of variant var (0: plain, 1: absorbing layer, 2:
+// B0, 3: B0 and absorbing layer); -1 for any other var.  The shared-memory limit must
 // have been raised by fused_batch_prepare_spec_t8.
 template <typename R, int C>
 int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int nitems, const BoxTable<R>& T,
@@ -1053,6 +1053,11 @@ int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int
     const size_t smem = Sizes<R, TY, Cfg<R, false, true>::LEAN>::BYTES;
     if (stage1) k_fused_batch_var<R, C, true, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
+  } else if (var == 2) {
+    constexpr int NT = Tile<TY, Cfg<R, true, false>::CPT>::NT;
+    const size_t smem = Sizes<R, TY, Cfg<R, true, false>::LEAN>::BYTES;
+    if (stage1) k_fused_batch_var<R, C, true, TY, 2><<<grid, NT, smem, st>>>(items, nitems, T);
+    else k_fused_batch_var<R, C, false, TY, 2><<<grid, NT, smem, st>>>(items, nitems, T);
   } else if (var == 3) {
     constexpr int NT = Tile<TY, Cfg<R, true, true>::CPT>::NT;
     const size_t smem = Sizes<R, TY, Cfg<R, true, true>::LEAN>::BYTES;
@@ -1082,6 +1087,9 @@ int fused_batch_prepare_spec_t8(int var) {
   } else if (var == 1) {
     k1 = k_fused_batch_var<R, C, true, TY, 1>;
     k2 = k_fused_batch_var<R, C, false, TY, 1>;
+  } else if (var == 2) {
+    k1 = k_fused_batch_var<R, C, true, TY, 2>;
+    k2 = k_fused_batch_var<R, C, false, TY, 2>;
   } else if (var == 3) {
     k1 = k_fused_batch_var<R, C, true, TY, 3>;
     k2 = k_fused_batch_var<R, C, false, TY, 3>;

@@ -101,8 +101,8 @@ int launch_fused_batch_t16(bool stage1, const BatchItem* items, int nitems, cons
 template <typename R, int C> int fused_batch_prepare_t8();
 template <typename R, int C> int fused_batch_prepare_t16();
 // Tile height 8, all grids of the launch of one B0 / absorbing-layer variant
-// var (bit 1: B0, bit 0: absorbing layer); specialised kernels exist for var
-// 0, 1 and 3 (launch returns -1, prepare 0, for var 2).
+// var (bit 1: B0, bit 0: absorbing layer), 0 <= var < 4 (launch returns -1,
+// prepare 0, for any other var).
 template <typename R, int C>
 int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int nitems, const BoxTable<R>& T,
                                int grid, cudaStream_t st);
