@@ -325,8 +325,9 @@ def run_reference(args):
 
 def bench_batch(args):
     """Batched workload: `--batch-boxes` boxes with sides U[48, 160] per axis
-    (half Alfven packets, half twisted flux tubes), `--steps` steps.  Times the
-    batch (autotuned tiling, one launch per stage for all boxes, CUDA graph)
+    (half Alfven packets, half twisted flux tubes; `--batch-kind packet`:
+    packets only), `--steps` steps.  Times the batch (autotuned tiling or
+    `--tile-y`, one launch per stage and variant for all boxes, CUDA graph)
     and the plain path that runs the same boxes one grid at a time, from the
     same initial state; reports both rates, time-to-result percentiles and the
     largest relative L2 difference between the two results."""

@@ -1030,8 +1030,10 @@ int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms) {
 // Batches (ffe_batch_*): many meshblocks advanced together.
 //
 // Members are split into groups of up to BATCH_MAX.  Each SSP-RK3 stage of a
-// group is ONE k_fused_batch launch over the work items (member, tile,
-// z-chunk) of all its members; every member has an entry (BatchBox) in the
+// group is one launch over the work items (member, tile, z-chunk) of all its
+// members of one B0 / absorbing-layer variant (k_fused_batch_var, tile height
+// 8), or of all its members (k_fused_batch, which switches per grid; tile
+// height 16, or a member's variant changed); every member has an entry (BatchBox) in the
 // launch's parameter table with its stage constants, its set pointers (the
 // member's own set rotation) and this step's boundary constants.  Pulsar
 // members add one batched fix-up (three launches) per stage, user_uniform

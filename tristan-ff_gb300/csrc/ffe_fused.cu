@@ -2,17 +2,18 @@
 // rk3Update (+ absorbing shell) + ghost fill + cleanEpar + ghost fill.
 //
 // A block owns a TX x TY column of cells and marches in z through a chunk of
-// planes.  Shared memory holds three plane rings:
+// planes.  Shared memory holds the plane rings (standard layout; the lean
+// layout of the plain FP32 variant is described at Rings):
 //   OLD (depth 5): stage-input E,B over the tile + 2 halo cells, one TMA box
 //                  per component and plane, fetched two planes ahead;
 //   EN  (depth 2): step-start E,B over the tile + 1 halo (stages 2 and 3),
 //                  fetched one plane ahead;
 //   NEW (depth 4): updated, not yet cleaned E,B over the tile + 1 halo.
-// Per plane k:  thread 0 issues TMA for OLD(k+3..k+4), EN(k+2);
+// Per plane k:  one thread issues TMA for OLD(k+3..k+4), EN(k+2);
 //               wait OLD(k+2), EN(k+1) -> NEW(k+1) = push + update on
-//               tile+1 (one thread per cell of the 34 x 10 region) ->
-//               barrier -> clean plane k on the tile from NEW(k-1..k+1),
-//               store E'' and B'.
+//               tile+1 (the 34 x 10 region, one or two cells per thread)
+//               -> barrier -> clean plane k on the tile from
+//               NEW(k-1..k+1), store E'' and B'.
 // With four NEW slots the clean of plane k and the push of plane k+2 touch
 // different slots, so one barrier per plane suffices and warps that have no
 // clean work move on to the next push.  A stage reads E,B (and the
@@ -74,15 +75,14 @@ constexpr int DN = 4;                    // NEW ring depth
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
-// rows (y0-1 .. y0+TY), NEW planes of NY rows.  Every shared plane has rows
-// of OW words.  A thread owns CPT cells stacked in y (rows CPT*q .. CPT*q +
+// rows (y0-1 .. y0+TY), NEW planes of NY rows; OLD and EN rows are OW words,
+// NEW rows NX words.  A thread owns CPT cells stacked in y (rows CPT*q .. CPT*q +
 // CPT-1 of the NEW region for the update, of the tile for the cleaning), so
 // the per-plane bookkeeping and the neighbour loads the cells share are paid
 // once for CPT cells.  The update threads are laid out on rows of TP (thread
 // t at x = t % TP, row group q = t / TP; lanes at x >= NX have no cell): TP =
-// OW for two cells per thread (FP32), so that a warp's lanes fall on
-// consecutive words of a row; TP = NX for one (FP64, whose double-rate pipe
-// is the limit), so that no lane idles.
+// OW for two cells per thread, so that a warp's lanes fall on consecutive
+// words of an OLD row; TP = NX for one, so that no lane idles.
 // TY = 8, CPT = 2: 34 x 10 = 340 cells on 5 row pairs, 192 threads (128 of
 // them also clean 32 x 8); CPT = 1: 340 cells, 352 threads.
 template <int TY, int CPT = 1>
@@ -93,8 +93,6 @@ struct Tile {
   static constexpr int NT = (TP * (NY / CPT) + 31) / 32 * 32;
   static constexpr int NCLEAN = TX * TY / CPT;  // threads that clean
 };
-// cells per thread of the single-grid kernel: two in FP32, which leaves room
-// for two blocks per SM at up to 168 registers; one in FP64
 // The batched kernel that switches variants per grid inlines the four B0 /
 // absorbing-layer variants of the body; with one cell per thread it stays at
 // two blocks per SM (TY = 8).
@@ -248,7 +246,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 
   const unsigned bar_old = smem_u32(bars), bar_en = smem_u32(bars + DO);
 
-  // ---- producer (thread 0): TMA copies of whole planes --------------------
+  // ---- producer (thread PRODUCER): TMA copies of whole planes -----------
   // OLD plane p lives in slot (p - kb + 2) % DO, EN plane p in (p - kb + 1) % DE.
   int old_next = kb - 2, en_next = kb - 1;
   const int old_last = ke + 1, en_last = ke;
