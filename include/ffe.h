@@ -272,11 +272,12 @@ int ffe_synchronize_timeout(ffe_t h, int32_t timeout_ms);
    fused path (path AUTO or FUSED; setup none, uniform, or psr with no
    periodic axis).  The batch does not own the handles; destroy it first.
    Each SSP-RK3 stage of all members is one kernel launch over the tiles of
-   every member (plus one batched launch per stage for user_uniform ghost
-   planes and three for the pulsar fix-up); the launches of a call are
-   captured into a CUDA graph and replayed.  Members keep their own set
-   rotation and step counter: results equal those of ffe_step on each member
-   with the same tiling.  stream: a cudaStream_t or NULL (own stream).     */
+   every member of one B0 / absorbing-layer variant (tile height 8), or of
+   every member (tile height 16), plus one batched launch per stage for
+   user_uniform ghost planes and three for the pulsar fix-up; the launches
+   of a call are captured into a CUDA graph and replayed.  Members keep
+   their own set rotation and step counter: results equal those of ffe_step
+   on each member.  stream: a cudaStream_t or NULL (own stream).           */
 typedef struct ffe_batch ffe_batch;
 typedef ffe_batch* ffe_batch_t;
 int ffe_batch_create(ffe_batch_t* out, const ffe_t* members, int32_t n, void* stream);
