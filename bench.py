@@ -1,11 +1,14 @@
 """Benchmark: cell-updates/s of the force-free SSP-RK3 step on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--size S] [--precision fp32|fp32c|fp64] [--no-cpu-baseline]
+                    [--size S] [--precision fp32c|fp32|fp32cd|fp64] [--no-cpu-baseline]
 
 Workload (the single-grid benchmark configuration): a periodic S^3 grid
 (S = 512), Bz = 1 plus 32 seeded Alfven and fast modes with integer
 wavevectors |k| <= 8 and amplitudes U[0, 0.02], c = 0.45, FP32 fields.
+The timed mode is FP32C (float storage, the increment form of the RK
+combination), the one that stays within 1e-5 of FP64; plain FP32 (the
+reference's arithmetic in float), FP32CD and FP64 are timed beside it.
 A step is one full main-loop body: three SSP-RK3 stages, each with its E
 cleaning and ghost fills.  One cell-update = one interior cell advanced one
 step.  Inputs are 3.3 GB per field set, far larger than the 129 MB L2, so no
@@ -18,11 +21,17 @@ Reported numbers:
             upload of E,B, K steps, download of E,B, all inside the timed region
             (median of three runs).
   roofline: the fused stage kernel (3 launches per step, the whole step):
-            algorithmic bytes = 48 words per cell-update (stage 1 reads E,B and
-            writes E,B; stages 2-3 also read the step-start E,B) / step time,
-            against the measured HBM copy bandwidth.
+            algorithmic bytes = 54 words per cell-update (18 per stage launch:
+            E,B in and out plus the step-start E,B) / step time, against the
+            measured HBM copy bandwidth; `frac_fused_words` restates it with
+            the 48 words the fused path must move (no step-start copy).
+  accuracy: relative L2 and L-infinity error of E and B of the timed mode
+            against the FP64 path after --accuracy-line-steps steps of the
+            same workload, and of the FP64 GPU path against the CPU oracle
+            (FP64) after --oracle-check-steps steps.
   cpu_baseline: the CPU restatement (oracle/, OpenMP, all host cores) on a
-            bounded sample of the same workload.
+            bounded sample of the same workload (the same grid, a few steps),
+            in the timed mode and in FP64, with the host's CPU model.
 Multi-GPU: replicas only (one independent grid per rank, no collective in the
 data path); value sums all ranks' cell-updates over the slowest rank's time.
 """
@@ -38,7 +47,12 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "tristan-ff_gb300"))
 
-WORDS_PER_CELL_STEP = 48      # fused path: 12 + 18 + 18 words per cell per step
+# Algorithmic words per cell-update: 3 stages x 18 (stage 1 reads E,B and
+# writes E,B and the step-start copy En,Bn; stages 2-3 read E,B,En,Bn and
+# write E,B), the compulsory traffic of a fully fused stage.  The fused path
+# keeps the step-start set in place (a set rotation) and so moves 48.
+WORDS_PER_CELL_STEP = 54
+WORDS_FUSED_PATH = 48
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -49,7 +63,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c", "fp32cd", "fp64"])
+    ap.add_argument("--precision", default="fp32c", choices=["fp32", "fp32c", "fp32cd", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-other-precisions", action="store_true",
                     help="skip the FP32C and FP64 timings added to the line (single GPU)")
@@ -74,6 +88,12 @@ def parse():
     ap.add_argument("--oracle-steps", type=int, default=0,
                     help="with --accuracy-steps: also check the FP64 GPU path against the CPU oracle "
                          "after this many steps")
+    ap.add_argument("--accuracy-line-steps", type=int, default=100,
+                    help="steps of the accuracy check added to the line (timed mode vs FP64; 0: none)")
+    ap.add_argument("--oracle-check-steps", type=int, default=10,
+                    help="steps of the FP64 GPU path vs the CPU oracle check added to the line (0: none)")
+    ap.add_argument("--cpu-steps", type=int, default=0,
+                    help="steps of the CPU baseline sample (0: 3 at 512^3, more on smaller grids)")
     return ap.parse_args()
 
 
@@ -203,7 +223,7 @@ def traffic_from_profile(precision, size):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -218,7 +238,7 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
@@ -257,68 +277,156 @@ def workload(size):
     return bg, modes
 
 
-def cpu_baseline(args, edge=None, steps=None, threads=None):
-    """Time the oracle (CPU restatement) on an edge^3 grid of the same workload."""
+def cpu_model():
+    """The host CPU's model name (lscpu), or the platform string."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, timeout=10).stdout
+        for line in out.decode(errors="replace").splitlines():
+            if line.strip().startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def time_oracle(size, prec, steps, threads, warm=1):
+    """Seconds per step of the oracle (CPU restatement, OpenMP, x-innermost
+    loops) on the random-mode workload of `size`, after `warm` untimed steps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import ffe
     import oracle as O
-    from ffe.workloads import random_modes, host_waves
+    from ffe.workloads import random_modes
     O.build()
-    threads = threads or os.cpu_count() or 1
-    edge = edge or args.cpu_sample or 128
-    steps = steps or 100
-    size = (edge, edge, edge)
     bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
-    prec = ffe.PRECISIONS[args.precision]
     o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
-    o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
+    o.init_waves(bg, modes)
     o.mainloop_prologue()
-    o.mainloop(1, 0)  # warm caches and pages
+    if warm:
+        o.mainloop(warm, 0)  # warm caches and pages
     t0 = time.perf_counter()
-    o.mainloop(steps, 1)
+    o.mainloop(steps, warm)
     dt = time.perf_counter() - t0
-    return {"value": edge ** 3 * steps / dt, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-            "sample": "%d^3 grid of the same random-mode workload, %d steps, %s, x-innermost loops, "
-                      "OpenMP %d threads, %.1f s" % (edge, steps, args.precision, threads, dt)}
+    o.close()
+    return dt / steps
+
+
+def cpu_baseline(args, edge=None, steps=None, threads=None):
+    """Time the oracle (CPU restatement) on a bounded sample of the workload:
+    the same grid, a few steps, in the timed mode and in FP64."""
+    import ffe
+    threads = threads or os.cpu_count() or 1
+    edge = edge or args.cpu_sample or args.size
+    steps = steps or args.cpu_steps or max(2, min(50, int(3 * (512.0 / edge) ** 3)))
+    size = (edge, edge, edge)
+    prec = ffe.PRECISIONS[args.precision]
+    s_step = time_oracle(size, prec, steps, threads)
+    s64 = time_oracle(size, ffe.FP64, max(1, steps // 2), threads)
+    return {"value": edge ** 3 / s_step, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+            "cpu": cpu_model(),
+            "sample": "%d^3 grid of the same random-mode workload, %d steps after 1 warm-up, %s, x-innermost "
+                      "loops, OpenMP %d threads, %.1f s" % (edge, steps, args.precision, threads, s_step * steps),
+            "fp64": {"value": edge ** 3 / s64, "unit": "cell-updates/s", "steps": max(1, steps // 2)}}
+
+
+def rel_errors(a, b):
+    """Relative L2 and L-infinity error of E and B of a against b (dicts of
+    interior arrays)."""
+    import numpy as np
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+    res = {}
+    for grp, comps in (("E", names[:3]), ("B", names[3:])):
+        num2 = den2 = linf = dmax = 0.0
+        for n in comps:
+            x = a[n].astype(np.float64)
+            y = b[n].astype(np.float64)
+            d = x - y
+            num2 += float(np.vdot(d, d).real)
+            den2 += float(np.vdot(y, y).real)
+            linf = max(linf, float(np.max(np.abs(d))))
+            dmax = max(dmax, float(np.max(np.abs(y))))
+        res[grp] = {"rel_l2": (num2 / den2) ** 0.5 if den2 else None, "rel_linf": linf / dmax if dmax else None}
+    return res
+
+
+def line_accuracy(args, size, bg, modes, stream):
+    """Accuracy of the timed mode, stated beside the timed number: relative L2
+    and L-infinity of E and B after --accuracy-line-steps steps against the
+    FP64 path from the same initial fields; and the FP64 GPU path against
+    the CPU oracle (FP64, OpenMP) after --oracle-check-steps steps.  The FP64
+    GPU path stands in for the oracle over the longer run once it matches
+    it over the short one."""
+    import ffe
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+    prec = ffe.PRECISIONS[args.precision]
+    n_acc, n_ora = args.accuracy_line_steps, args.oracle_check_steps
+    out = {}
+    g64 = ffe.Solver(ffe.make_desc(size, precision=ffe.FP64, stream=stream))
+    g64.init_waves(bg, modes)
+    g64.mainloop_prologue()
+    done = 0
+    if n_ora:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        init = g64.fields()
+        o = O.Oracle(ffe.make_desc(size, precision=ffe.FP64), threads=os.cpu_count() or 1, loop_order=1)
+        o.set_fields(init)
+        del init
+        g64.mainloop(n_ora, 0)
+        done = n_ora
+        t0 = time.perf_counter()
+        o.mainloop(n_ora, 0)
+        t_ora = time.perf_counter() - t0
+        cpu = {n: ffe.interior(o.download(n)) for n in names}
+        o.close()
+        gpu = {n: ffe.interior(a) for n, a in g64.fields().items()}
+        out["fp64_gpu_vs_cpu_oracle"] = dict(rel_errors(gpu, cpu), steps=n_ora, oracle_seconds=round(t_ora, 1))
+        del cpu, gpu
+    if n_acc and prec != ffe.FP64:
+        g = ffe.Solver(ffe.make_desc(size, precision=prec, stream=stream))
+        g.init_waves(bg, modes)
+        g.mainloop_prologue()
+        g.mainloop(n_acc, 0)
+        mine = {n: ffe.interior(a) for n, a in g.fields().items()}
+        g.close()
+        g64.mainloop(n_acc - done, done)
+        ref = {n: ffe.interior(a) for n, a in g64.fields().items()}
+        out["vs_fp64"] = dict(rel_errors(mine, ref), steps=n_acc, mode=args.precision,
+                              reference="the FP64 GPU path from the same initial fields")
+    g64.close()
+    return out
 
 
 def run_reference(args):
-    """The reference's CPU path: its Fortran build is unavailable here, so the
-    CPU restatement of the same procedures (oracle/) runs on all host cores."""
+    """The reference's CPU path: its Fortran build is unavailable (no Fortran
+    compiler, MPI or HDF5 in this image or on the GPU hosts), so the CPU
+    restatement of the same procedures (oracle/) runs on all host cores, on
+    the benchmark grid itself (--size, 512^3 by default), in the reference's
+    arithmetic (FP32: its default real)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    edge = args.cpu_sample or 128
-    import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ffe
-    import oracle as O
-    from ffe.workloads import random_modes, host_waves
-    O.build()
+    edge = args.cpu_sample or args.size
     threads = os.cpu_count() or 1
     size = (edge, edge, edge)
-    bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
-    prec = ffe.PRECISIONS[args.precision]
-    o = O.Oracle(ffe.make_desc(size, precision=prec), threads=threads, loop_order=1)
-    o.set_fields(host_waves(size, bg, modes, np.float64 if prec == ffe.FP64 else np.float32))
-    o.mainloop_prologue()
-    o.mainloop(args.warmup, 0)
-    t0 = time.perf_counter()
-    o.mainloop(args.steps, args.warmup)
-    dt = time.perf_counter() - t0
-    v = edge ** 3 * args.steps / dt
-    cfg = {"workload": "random Alfven+fast modes, periodic %d^3 (CPU sample %d^3)" % (args.size, edge),
+    s_step = time_oracle(size, ffe.FP32, args.steps, threads, warm=args.warmup)
+    v = edge ** 3 / s_step
+    cfg = {"workload": "random Alfven+fast modes, periodic %d^3" % edge
+                       + ("" if edge == args.size else " (CPU sample of the %d^3 grid)" % args.size),
            "grid": [args.size] * 3, "modes": 32, "kmax": 8, "amax": 0.02, "cc": 0.45,
            "boundary": "periodic", "parallelism": "replicas" if world > 1 else "single grid"}
     line = {"metric": "cell-updates/s per RK3 step", "value": v, "unit": "cell-updates/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * s_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic", "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-                             "sample": "%d^3 grid, %d steps after %d warm-up; the reference's Fortran build "
-                                       "is unavailable (no Fortran compiler, MPI, HDF5), so its CPU "
-                                       "restatement runs" % (edge, args.steps, args.warmup)},
+                             "cpu": cpu_model(),
+                             "sample": "%d^3 grid, %d steps after %d warm-up, fp32 (the reference's real); the "
+                                       "reference's Fortran build is unavailable (no Fortran compiler, MPI, "
+                                       "HDF5), so its CPU restatement runs" % (edge, args.steps, args.warmup)},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -644,12 +752,15 @@ def main():
     traffic = traffic_from_profile(args.precision, S)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "k_fused (fused stage, %d launches/step = whole step)" % launches_per_step,
-            "alg_bytes_per_launch": alg_bytes_step / 3, "peak_source": peak_kind + " copy bandwidth"}
+            "alg_bytes_per_launch": alg_bytes_step / 3, "words_per_cell_update": WORDS_PER_CELL_STEP,
+            "frac_fused_words": achieved / peak * WORDS_FUSED_PATH / WORDS_PER_CELL_STEP,
+            "peak_source": peak_kind + " copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6800 GB/s"}
     others = {}
     if world == 1 and not args.no_other_precisions:
         # the same workload in the other precisions, for the FP32-vs-FP64 comparison of the metric
         g.close()
-        for name, k, w in (("fp32c", 10, 2), ("fp64", 4, 1)):
+        for name, k, w in (("fp32", 10, 2), ("fp32c", 10, 2), ("fp32cd", 4, 1), ("fp64", 4, 1)):
             if name == args.precision:
                 continue
             h = ffe.Solver(ffe.make_desc(size, precision=ffe.PRECISIONS[name], stream=stream.cuda_stream))
@@ -665,6 +776,13 @@ def main():
             ms = e0.elapsed_time(e1) / k
             others[name] = {"value": cells / (ms / 1e3), "ms_per_step": ms, "steps": k, "warmup": w}
             h.close()
+    acc = None
+    if world == 1 and (args.accuracy_line_steps or args.oracle_check_steps):
+        try:
+            g.close()
+            acc = line_accuracy(args, size, bg, modes, stream.cuda_stream)
+        except Exception as e:
+            acc = {"error": str(e)[:200]}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
@@ -682,7 +800,7 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": "synthetic", "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks, "gpu_launches": launches_per_step * args.steps, "finite": ok,
-            "other_precisions": others}
+            "accuracy": acc, "other_precisions": others}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()

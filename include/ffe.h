@@ -215,13 +215,20 @@ int ffe_init_waves(ffe_t h, const double bg[3], int32_t nmodes, const double* mo
    a run loop where an allocation call, which may synchronise the device or
    fail on fragmented memory, is not acceptable).  ex..bz are device pointers
    to arrays in the reference's layout ((sx+4)(sy+4)(sz+4), x fastest, cell
-   -2 first); E is cleaned in place.  The out-of-place scratch is a fixed
+   -2 first); E is cleaned in place.  The cleaning is the reference's, with
+   no TINY in the B^2 denominators: it equals ffe_clean_epar on a handle
+   created without FFE_FLAG_CLEAN_TINY.  The out-of-place scratch is a fixed
    24 MiB device array inside the library, so 3*sx*sy*sz values must fit
    (2,097,152 interior cells in FP32, 1,048,576 in FP64); larger sizes
-   return FFE_EINVAL.  The first call on a device looks up the scratch's
-   device address (make it before any stream capture).  All calls share the
-   scratch: calls that overlap on the GPU race.  Asynchronous on `stream`
-   (a cudaStream_t, NULL = the default stream); errors read back with
+   return FFE_EINVAL.  CUDA loads the library's modules lazily, so the
+   scratch takes its 24 MiB of device memory when first needed on a device.
+   A call with sx = sy = sz = 0 and every pointer NULL does only that set-up
+   on the current device (loads the scratch and the kernels, looks up the
+   scratch's device address) and returns FFE_OK.  Make it before reserving
+   the rest of HBM and before any stream capture; otherwise the first
+   cleaning call on the device does it.  All calls share the scratch: calls
+   that overlap on the GPU race.  Asynchronous on `stream` (a cudaStream_t,
+   NULL = the default stream); errors read back with
    ffe_last_error(NULL, ...).                                               */
 int ffe_clean_epar_noalloc(int32_t sx, int32_t sy, int32_t sz, int32_t precision, void* ex, void* ey, void* ez,
                            const void* bx, const void* by, const void* bz, void* stream);

@@ -56,6 +56,8 @@ def load():
         lib.ora_exchange.argtypes = [V, ctypes.c_int]
         lib.ora_user_bc.argtypes = [V, ctypes.c_int]
         lib.ora_step.argtypes = [V, ctypes.c_int, ctypes.c_int]
+        lib.ora_init_waves.argtypes = [V, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_double)]
         _lib = lib
     return _lib
 
@@ -138,6 +140,15 @@ class Oracle:
         self.lib.ora_step(self.h, steps, step0)
 
     step = mainloop
+
+    def init_waves(self, bg, modes):
+        """Synthetic plane-wave fields (same formula as ffe.Solver.init_waves;
+        the sines come from products of per-axis exponentials, so values may
+        differ from the library's in the last bit: for timing samples)."""
+        import numpy as np
+        bgv = (ctypes.c_double * 3)(*[float(x) for x in bg])
+        m = np.ascontiguousarray(np.asarray(modes, np.float64).reshape(-1, 11))
+        self.lib.ora_init_waves(self.h, bgv, m.shape[0], m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
 
     def synchronize(self, timeout_ms=None):
         pass

@@ -1,8 +1,13 @@
-/* The C ABI from plain C (what a Fortran iso_c_binding module binds): create a
-   periodic 48x32x24 FP32 meshblock, upload a uniform Bz plus a small Ex ripple,
-   run the prologue and 10 fused steps, download, check finiteness and that the
-   uniform field is kept; then the batch and output entry points on the same
-   handle.  Exit status 0 on success.  Built and run by tests/test_c_abi.py. */
+/* The C ABI from plain C (what a Fortran iso_c_binding module binds).
+   Part 1: a periodic 16x12x8 FP32 meshblock on the fused-exact path, inputs
+   from an exact integer formula (the same as cabi_fields in
+   tests/golden/make_golden.py), the prologue and 3 steps; E and B are
+   written raw to the file named by argv[1], which tests/test_c_abi.py
+   compares bit for bit with the golden fixture cabi_fp32_periodic.
+   Part 2: a periodic 48x32x24 FP32 meshblock, a uniform Bz plus a small Ex
+   ripple, 10 fused steps, finiteness and the uniform field kept; then the
+   batch and output entry points on the same handle.
+   Exit status 0 on success. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -19,7 +24,56 @@
     }                                                                     \
   } while (0)
 
-int main(void) {
+/* value of the golden input formula at ghosted-array position i */
+static float cabi(size_t i, unsigned mul, unsigned mod, int off, float den, float base) {
+  return base + (float)((int)((i * mul) % mod) - off) / den;
+}
+
+static int golden_part(const char* path) {
+  ffe_grid_desc d;
+  CHECK(ffe_desc_default(&d, 16, 12, 8));
+  d.precision = FFE_FP32;
+  d.path = FFE_PATH_FUSED_EXACT;
+  ffe_t h = NULL;
+  CHECK(ffe_create(&h, &d));
+  size_t n = 0;
+  CHECK(ffe_field_elems(h, &n));
+  float* f[6];
+  for (int c = 0; c < 6; ++c) f[c] = malloc(n * sizeof(float));
+  for (size_t i = 0; i < n; ++i) {
+    f[0][i] = cabi(i, 37, 101, 50, 4096.0f, 0.0f);
+    f[1][i] = cabi(i, 53, 97, 48, 4096.0f, 0.0f);
+    f[2][i] = cabi(i, 29, 89, 44, 4096.0f, 0.0f);
+    f[3][i] = cabi(i, 17, 83, 41, 8192.0f, 0.0f);
+    f[4][i] = cabi(i, 41, 79, 39, 8192.0f, 0.0f);
+    f[5][i] = cabi(i, 13, 73, 36, 8192.0f, 1.0f);
+  }
+  int32_t ids[6] = {FFE_EX, FFE_EY, FFE_EZ, FFE_BX, FFE_BY, FFE_BZ};
+  const void* up[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
+  void* down[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
+  CHECK(ffe_upload_many(h, 6, ids, up, n));
+  CHECK(ffe_mainloop_prologue(h));
+  CHECK(ffe_step(h, 3, 0));
+  CHECK(ffe_download_many(h, 6, ids, down, n));
+  CHECK(ffe_destroy(h));
+  FILE* out = fopen(path, "wb");
+  if (!out) {
+    fprintf(stderr, "cannot write %s\n", path);
+    return 1;
+  }
+  for (int c = 0; c < 6; ++c) {
+    if (fwrite(f[c], sizeof(float), n, out) != n) {
+      fclose(out);
+      return 1;
+    }
+    free(f[c]);
+  }
+  fclose(out);
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc > 1 && golden_part(argv[1]) != 0) return 1;
   ffe_grid_desc d;
   CHECK(ffe_desc_default(&d, 48, 32, 24));
   d.precision = FFE_FP32;

@@ -37,6 +37,18 @@ def rand_fields(size, dt, seed):
     return f
 
 
+def cabi_fields(size):
+    """Inputs of the plain-C ABI program (tests/c/abi_roundtrip.c): small
+    integers over powers of two, exact in float32, indexed by the element's
+    position i in the ghosted array, so C and numpy give identical values."""
+    shp = (size[2] + 4, size[1] + 4, size[0] + 4)
+    i = np.arange(int(np.prod(shp)), dtype=np.int64)
+    def f(mul, mod, off, den, base=0.0):
+        return (base + ((i * mul) % mod - off).astype(np.float32) / np.float32(den)).astype(np.float32).reshape(shp)
+    return {"ex": f(37, 101, 50, 4096), "ey": f(53, 97, 48, 4096), "ez": f(29, 89, 44, 4096),
+            "bx": f(17, 83, 41, 8192), "by": f(41, 79, 39, 8192), "bz": f(13, 73, 36, 8192, 1.0)}
+
+
 CASES = [
     # name, size, precision, boundary, setup, params, steps, input kind
     ("alfven_fp64_periodic", (16, 4, 4), ffe.FP64, (1, 1, 1), 0, (), 10, "alfven"),
@@ -47,6 +59,7 @@ CASES = [
     ("psr_fp64_open", (20, 20, 20), ffe.FP64, (0, 0, 0), 1, (4.0, 30.0, 120.0, 1.0), 3, "setup"),
     ("uniform_fp32_tube", (12, 12, 10), ffe.FP32, (1, 1, 0), 2, (8.0, 0.4, 5.0, 0.3), 3, "setup"),
     ("loop_fp64", (12, 12, 10), ffe.FP64, (1, 1, 0), 3, (3.0, 1.0, 1.0, 0.5, 5.0, 0.3), 3, "setup"),
+    ("cabi_fp32_periodic", (16, 12, 8), ffe.FP32, (1, 1, 1), 0, (), 3, "cabi"),
 ]
 
 
@@ -60,6 +73,9 @@ def main():
         if kind == "alfven":
             bg, modes, _ = alfven_packet(size, seed=0, amp=0.1)
             f = host_waves(size, bg, modes, dt)
+            o.set_fields(f)
+        elif kind == "cabi":
+            f = cabi_fields(size)
             o.set_fields(f)
         elif kind == "random":
             f = rand_fields(size, dt, seed=sum(map(ord, name)))

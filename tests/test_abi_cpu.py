@@ -89,3 +89,13 @@ def test_footprint_query_needs_no_gpu(lib):
     assert ffe.desc_device_bytes(ffe.make_desc((46000, 46000, 2))) > 0
     with pytest.raises(ffe.FFEError):
         ffe.desc_device_bytes(ffe.make_desc((50000, 50000, 2)))
+
+
+def test_descriptor_rejects_grids_beyond_the_launch_limits(lib):
+    """The per-cell kernels put the z planes (ghosts included) on a grid's z
+    dimension: a block taller than 65531 cells is refused with a clear message
+    instead of failing at its first launch."""
+    assert ffe.desc_device_bytes(ffe.make_desc((2, 2, 65531))) > 0
+    with pytest.raises(ffe.FFEError) as e:
+        ffe.desc_device_bytes(ffe.make_desc((2, 2, 65532)))
+    assert "65535" in str(e.value)

@@ -1,0 +1,99 @@
+"""The single-grid benchmark configurations at their own sizes and step counts.
+
+* 64^3 Alfven packet, FP64, periodic, 1000 steps (the smallest configuration,
+  the one the reference's CPU build runs): the GPU against the CPU oracle,
+  which restates src/algorithms/field_solver.F90:15-335 in the stage order of
+  src/tristanmainloop.F90:44-84.  The fused-exact path (no multiply-add
+  contraction, correctly rounded division) equals the oracle bit for bit after
+  all 1000 steps; the default fused path (contraction, fast quotients in FP32
+  only) stays within 1e-12 relative L2.
+* 512^3 random-mode grid, 100 steps: FP32C (the timed mode) against the FP64
+  path within 1e-5 relative L2 of E and of B; and the FP64 GPU path against
+  the FP64 CPU oracle over 10 steps within 1e-12, which is what lets the FP64
+  GPU path stand in for the oracle at this size.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ffe
+from conftest import rel_l2, rel_linf
+from ffe.workloads import alfven_packet, random_modes
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ("ex", "ey", "ez", "bx", "by", "bz")
+
+
+def _grouped(a, b):
+    """Relative L2 of E and of B (interiors), a against b."""
+    out = {}
+    for grp, comps in (("E", NAMES[:3]), ("B", NAMES[3:])):
+        x = np.concatenate([ffe.interior(a[n]).ravel().astype(np.float64) for n in comps])
+        y = np.concatenate([ffe.interior(b[n]).ravel().astype(np.float64) for n in comps])
+        out[grp] = (rel_l2(x, y), rel_linf(x, y))
+    return out
+
+
+def test_alfven_packet_64_fp64_1000_steps_matches_oracle(oracle_mod):
+    size = (64, 64, 64)
+    bg, modes, _ = alfven_packet(size, seed=0, amp=0.1)
+    steps = 1000
+    o = oracle_mod.Oracle(ffe.make_desc(size, precision=ffe.FP64), threads=os.cpu_count() or 1)
+    got = {}
+    for path in (ffe.PATH_FUSED_EXACT, ffe.PATH_FUSED):
+        g = ffe.Solver(ffe.make_desc(size, precision=ffe.FP64, path=path))
+        g.init_waves(bg, modes)
+        if path == ffe.PATH_FUSED_EXACT:
+            o.set_fields(g.fields())
+        g.mainloop_prologue()
+        g.mainloop(steps, 0)
+        g.synchronize(timeout_ms=120000)
+        got[path] = g.fields()
+        g.close()
+    o.mainloop_prologue()
+    o.mainloop(steps, 0)
+    want = o.fields()
+    o.close()
+    for n in NAMES:
+        assert np.array_equal(got[ffe.PATH_FUSED_EXACT][n], want[n]), \
+            (n, float(np.max(np.abs(got[ffe.PATH_FUSED_EXACT][n] - want[n]))))
+    err = _grouped(got[ffe.PATH_FUSED], want)
+    assert err["E"][0] <= 1e-12 and err["B"][0] <= 1e-12, err
+    # the packet is still there after crossing the box 15 times (the Yee
+    # scheme does not damp a linear wave)
+    assert 0.05 < float(np.max(np.abs(ffe.interior(want["by"])))) < 0.15
+
+
+def test_random_modes_512_fp32c_within_1e5_of_fp64(oracle_mod):
+    torch = pytest.importorskip("torch")
+    free, _ = torch.cuda.mem_get_info()
+    if free < 60e9:
+        pytest.skip("needs ~40 GB of free device memory")
+    size = (512, 512, 512)
+    bg, modes, _ = random_modes(size, seed=1, n=32, kmax=8, amax=0.02)
+
+    g64 = ffe.Solver(ffe.make_desc(size, precision=ffe.FP64))
+    g64.init_waves(bg, modes)
+    g64.mainloop_prologue()
+    # FP64 GPU against the FP64 CPU oracle, 10 steps
+    o = oracle_mod.Oracle(ffe.make_desc(size, precision=ffe.FP64), threads=os.cpu_count() or 1)
+    o.set_fields(g64.fields())
+    o.mainloop_prologue()
+    g64.mainloop(10, 0)
+    o.mainloop(10, 0)
+    err = _grouped(g64.fields(), o.fields())
+    o.close()
+    assert err["E"][0] <= 1e-12 and err["B"][0] <= 1e-12, err
+
+    # FP32C against the FP64 GPU path, 100 steps
+    g32 = ffe.Solver(ffe.make_desc(size, precision=ffe.FP32C))
+    g32.init_waves(bg, modes)
+    g32.mainloop_prologue()
+    g32.mainloop(100, 0)
+    g64.mainloop(90, 10)
+    err = _grouped(g32.fields(), g64.fields())
+    g32.close()
+    g64.close()
+    assert err["E"][0] <= 1e-5 and err["B"][0] <= 1e-5, err

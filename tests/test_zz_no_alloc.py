@@ -6,7 +6,8 @@ The caller's arrays here are torch CUDA tensors in the reference's layout; the
 test calls the new entry point through the C ABI twice in a row and checks each
 result against the existing entry point (ffe_clean_epar on a handle), bit for
 bit as the staged parity tests do (both run the same cleaning arithmetic with
-no multiply-add contraction).  It then checks that a size beyond the 24 MiB
+no multiply-add contraction).  It also checks the set-up call (after it, a
+cleaning call takes no device memory), and that a size beyond the 24 MiB
 scratch is refused with a clear message.
 """
 import ctypes
@@ -19,6 +20,7 @@ import ffe
 pytestmark = pytest.mark.gpu
 
 F3 = ("ex", "ey", "ez")
+SCRATCH_BYTES = 24 << 20
 
 
 def _fields(size, dt, seed):
@@ -29,7 +31,33 @@ def _fields(size, dt, seed):
     return f
 
 
-@pytest.mark.parametrize("prec", [ffe.FP32, ffe.FP64, ffe.FP32C])
+def _clean(lib, size, prec, dev, stream):
+    return lib.ffe_clean_epar_noalloc(size[0], size[1], size[2], prec,
+                                      dev["ex"].data_ptr(), dev["ey"].data_ptr(), dev["ez"].data_ptr(),
+                                      dev["bx"].data_ptr(), dev["by"].data_ptr(), dev["bz"].data_ptr(),
+                                      stream)
+
+
+def test_clean_epar_noalloc_setup_then_no_device_memory():
+    torch = pytest.importorskip("torch")
+    lib = ffe.load_library()
+    size = (40, 24, 12)
+    f = _fields(size, np.float32, seed=3)
+    dev = {n: torch.from_numpy(a.copy()).cuda() for n, a in f.items()}
+    torch.cuda.synchronize()
+    rc = lib.ffe_clean_epar_noalloc(0, 0, 0, ffe.FP32, None, None, None, None, None, None, None)
+    assert rc == 0, ffe._last_error(lib, None)
+    free0, _ = torch.cuda.mem_get_info()
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        assert _clean(lib, size, ffe.FP32, dev, stream) == 0, ffe._last_error(lib, None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    # the scratch was placed by the set-up call: the cleanings took none of it
+    assert free0 - free1 < SCRATCH_BYTES, (free0, free1)
+
+
+@pytest.mark.parametrize("prec", [ffe.FP32, ffe.FP64, ffe.FP32C, ffe.FP32CD])
 def test_clean_epar_noalloc_matches_handle_path(prec):
     torch = pytest.importorskip("torch")
     lib = ffe.load_library()
@@ -50,10 +78,7 @@ def test_clean_epar_noalloc_matches_handle_path(prec):
     dev = {n: torch.from_numpy(a.copy()).cuda() for n, a in f.items()}
     stream = torch.cuda.current_stream().cuda_stream
     for want in (want1, want2):
-        rc = lib.ffe_clean_epar_noalloc(size[0], size[1], size[2], prec,
-                                        dev["ex"].data_ptr(), dev["ey"].data_ptr(), dev["ez"].data_ptr(),
-                                        dev["bx"].data_ptr(), dev["by"].data_ptr(), dev["bz"].data_ptr(),
-                                        stream)
+        rc = _clean(lib, size, prec, dev, stream)
         assert rc == 0, ffe._last_error(lib, None)
         torch.cuda.synchronize()
         for n in F3:
@@ -62,6 +87,29 @@ def test_clean_epar_noalloc_matches_handle_path(prec):
     # B is read only
     for n in ("bx", "by", "bz"):
         assert np.array_equal(dev[n].cpu().numpy(), f[n])
+
+
+def test_clean_epar_noalloc_tall_block():
+    """sz beyond the 65,535 blocks a grid's z dimension allows (a handle
+    refuses such a block): the kernels loop over cells, so it is cleaned like
+    any other; checked against the oracle's cleanEpar, which the handle path
+    matches bit for bit."""
+    torch = pytest.importorskip("torch")
+    import oracle as O
+    lib = ffe.load_library()
+    size = (2, 2, 70000)
+    f = _fields(size, np.float32, seed=9)
+    o = O.Oracle(ffe.make_desc(size, precision=ffe.FP32))
+    o.set_fields(f)
+    o.cleanEpar()
+    want = {n: o.download(n) for n in F3}
+    o.close()
+    dev = {n: torch.from_numpy(a.copy()).cuda() for n, a in f.items()}
+    assert _clean(lib, size, ffe.FP32, dev, torch.cuda.current_stream().cuda_stream) == 0, \
+        ffe._last_error(lib, None)
+    torch.cuda.synchronize()
+    for n in F3:
+        assert np.array_equal(dev[n].cpu().numpy(), want[n]), n
 
 
 def test_clean_epar_noalloc_rejects_oversize():

@@ -531,6 +531,10 @@ int validate_desc(ffe_grid_desc& d) {
   // the fused kernels hold in-plane offsets in 32 bits
   if ((long long)(d.sx + 2 * FFE_NGHOST + 64) * (d.sy + 2 * FFE_NGHOST) >= (1LL << 31))
     return set_thread_err(FFE_EINVAL, "a plane of more than 2^31 elements is not supported");
+  // the per-cell kernels put z planes (ghosts included) on the grid's z
+  // dimension and 8-row groups on its y dimension, each at most 65535 blocks
+  if (d.sz + 2 * FFE_NGHOST > 65535 || (d.sy + 2 * FFE_NGHOST + 7) / 8 > 65535)
+    return set_thread_err(FFE_EINVAL, "sz + 4 must be <= 65535 and sy + 4 <= 524280 (kernel grid limits)");
   // one absorbing axis makes all three absorbing (src/logistics/initialize.F90:144-148)
   if (d.boundary[0] == 2 || d.boundary[1] == 2 || d.boundary[2] == 2)
     d.boundary[0] = d.boundary[1] = d.boundary[2] = 2;
