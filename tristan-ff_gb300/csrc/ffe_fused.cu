@@ -85,12 +85,19 @@ constexpr long long WAIT_LIMIT = 1LL << 22;
 // words of an OLD row; TP = NX for one, so that no lane idles.
 // TY = 8, CPT = 2: 34 x 10 = 340 cells on 5 row pairs, 192 threads (128 of
 // them also clean 32 x 8); CPT = 1: 340 cells, 352 threads.
+// With two cells per thread the update threads are laid out one warp per
+// row pair (WR): warp w < NY/2 takes x = 0..31 of the NEW region's row pair w,
+// so that its 32 lanes read 32 consecutive words of each OLD row and write 32
+// consecutive words of each NEW row (no shared-memory bank conflict), and the
+// lanes of the last warp take the two remaining columns of every row pair.
 template <int TY, int CPT = 1>
 struct Tile {
   static constexpr int OH = TY + 4, EH = TY + 2, NY = TY + 2;
   static_assert(NY % CPT == 0 && TY % CPT == 0, "cells per thread must divide the tile rows");
+  static constexpr bool WR = CPT == 2;
+  static constexpr int RG = NY / CPT;  // row groups of the NEW region
   static constexpr int TP = CPT == 1 ? NX : OW;
-  static constexpr int NT = (TP * (NY / CPT) + 31) / 32 * 32;
+  static constexpr int NT = WR ? (RG + (2 * RG + 31) / 32) * 32 : (TP * RG + 31) / 32 * 32;
   static constexpr int NCLEAN = TX * TY / CPT;  // threads that clean
 };
 // The batched kernel that switches variants per grid inlines the four B0 /
@@ -98,40 +105,51 @@ struct Tile {
 // two blocks per SM (TY = 8).
 constexpr int BATCH_CPT = 1;
 
-// Ring layout.  Standard (FP64, the B0 and absorbing-layer variants, the
-// per-grid-switch batched kernel): OLD ring of 5 planes (two planes of copies
-// ahead of use), step-start fields in a 2-plane TMA ring.  Lean (the plain
-// FP32 variant): OLD ring of 4 planes (one plane ahead), step-start fields
-// loaded by each thread for its own cells into registers one plane ahead:
-// 74 KB of shared memory at TY = 8, so that three blocks fit on an SM.  NEW
-// rows are NX words in both.
-template <bool LEAN>
+// Ring layout by kind RK.  0, standard (FP64, the B0 and absorbing-layer
+// variants, the per-grid-switch batched kernel): OLD ring of 5 planes (two
+// planes of copies ahead of use), step-start fields in a 2-plane TMA ring.
+// 1, lean (the plain FP32 variant): OLD ring of 4 planes (one plane ahead),
+// step-start fields loaded by each thread for its own cells into registers
+// one plane ahead: 74 KB of shared memory at TY = 8.  NEW rows are NX words
+// in both.
+template <int RK>
 struct Rings {
-  static constexpr int DO = LEAN ? 4 : 5, DE = LEAN ? 0 : 2;
+  static constexpr int DO = RK == 1 ? 4 : 5, DE = RK == 0 ? 2 : 0;
   static constexpr int NP = NX;  // NEW row pitch
 };
 
-// Configuration of the single-variant kernels (k_fused, k_fused_batch_var)
-// by element type and variant: the plain FP32 variant (no B0, no absorbing
-// layer) takes two cells per thread and lean rings at three blocks per SM (96
-// registers); the B0 and absorbing-layer variants, measured slower in that
-// form (a 160^3 pulsar stage: 321 us against 215 us), and FP64 take one cell
-// per thread and the standard rings (two blocks per SM in FP32, one in FP64).
-template <typename R, bool B0, bool ABS = false>
-struct Cfg {
-  static constexpr bool LEAN = sizeof(R) == 4 && !B0 && !ABS;
-  static constexpr int CPT = LEAN ? 2 : 1;
-  static constexpr int MINB = LEAN ? 3 : (sizeof(R) == 4 ? 2 : 1);
-};
-
-template <typename R, int TY, bool LEAN = false> struct Sizes {
+template <typename R, int TY, int RK = 0> struct Sizes {
   static constexpr int OLDBOX = ((OW * Tile<TY>::OH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
   static constexpr int ENBOX = ((OW * Tile<TY>::EH * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);
-  static constexpr int NEWPL = Tile<TY>::NY * Rings<LEAN>::NP;  // one component of one NEW plane
-  static constexpr int OLD = Rings<LEAN>::DO * 6 * OLDBOX;
-  static constexpr int EN = Rings<LEAN>::DE * 6 * ENBOX;
+  static constexpr int NEWPL = Tile<TY>::NY * Rings<RK>::NP;  // one component of one NEW plane
+  static constexpr int OLD = Rings<RK>::DO * 6 * OLDBOX;
+  static constexpr int EN = Rings<RK>::DE * 6 * ENBOX;
   static constexpr int NEW = DN * 6 * NEWPL;
-  static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * (Rings<LEAN>::DO + Rings<LEAN>::DE);
+  static constexpr int BARS = Rings<RK>::DO + Rings<RK>::DE;
+  static constexpr size_t BYTES = sizeof(R) * (size_t)(OLD + EN + NEW) + 8 * BARS;
+};
+
+// Configuration of the single-variant kernels (k_fused, k_fused_batch_var)
+// by element type, precision mode C, variant and tile height: the plain FP32
+// variant (no B0, no absorbing layer) takes two cells per thread and the lean
+// rings; on the fast path (C != 2) it evaluates both cells at once with the
+// paired FP32 instructions (PK), which needs up to 168 registers (two blocks
+// per SM); the single-grid kernel runs it at tile height PLAIN_TY (12: two
+// blocks per SM by shared memory), the batched kernels at 8, where the exact
+// path and FP32CD run at three blocks per SM (96 registers); the B0 and
+// absorbing-layer variants, measured slower with two
+// cells per thread (a 160^3 pulsar stage: 321 us against 215 us), and FP64
+// take one cell per thread and the standard rings (two blocks per SM in FP32,
+// one in FP64).
+template <typename R, int C, bool B0, bool ABS, int TY>
+struct Body {
+  static constexpr bool LEAN = sizeof(R) == 4 && !B0 && !ABS;
+  static constexpr int CPT = LEAN ? 2 : 1;
+  static constexpr bool PK = LEAN && FFE_FAST && C != 2;
+  static constexpr int RK = LEAN ? 1 : 0;
+  static constexpr int NT = Tile<TY, CPT>::NT;
+  static constexpr int MINB = (PK || (LEAN && TY > 8)) ? 2 : (LEAN ? 3 : (sizeof(R) == 4 ? 2 : 1));
+  static constexpr size_t SMEM = Sizes<R, TY, RK>::BYTES;
 };
 
 // Accessor over global arrays around linear index s (used for halo cells that
@@ -202,24 +220,45 @@ struct SmemOld {
 };
 
 // Accessor over the NEW ring for clean_cell.
-template <typename R, int TY, bool LEAN>
+template <typename R, int TY, int RK>
 struct SmemNew {
   const R* b[3];
   __device__ __forceinline__ R operator()(int c, int di, int djj, int dkk) const {
-    return b[dkk + 1][c * Sizes<R, TY, LEAN>::NEWPL + djj * Rings<LEAN>::NP + di];
+    return b[dkk + 1][c * Sizes<R, TY, RK>::NEWPL + djj * Rings<RK>::NP + di];
+  }
+};
+
+// Accessors over the OLD and NEW rings for the packed two-cell forms:
+// float2 {value at the thread's lower cell, value at its upper cell}.
+template <int TY>
+struct SmemOldPair {
+  const float* b[3];
+  __device__ __forceinline__ float2 operator()(int c, int di, int djj, int dkk) const {
+    const float* q = b[dkk + 1] + (c * Sizes<float, TY>::OLDBOX + djj * OW + di);
+    return make_float2(q[0], q[OW]);
+  }
+};
+template <int TY>
+struct SmemNewPair {
+  const float* b[3];
+  __device__ __forceinline__ float2 operator()(int c, int di, int djj, int dkk) const {
+    const float* q = b[dkk + 1] + (c * Sizes<float, TY, 1>::NEWPL + djj * Rings<1>::NP + di);
+    return make_float2(q[0], q[Rings<1>::NP]);
   }
 };
 
 // One block's work: the TX x TY column (tile_x, tile_y) of a grid, planes of
 // z-chunk `chunk`.  Shared by the single-grid kernel and the batched kernel.
 // mi / me: the six tensor maps of the stage-input and step-start sets.
+// RK: ring kind (0 standard, 1 lean; see Rings).
 // Returns false when a wait on a copy gave up (the error word is set).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT, bool LEAN>
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT, int RK>
 __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensorMap* me, const Params<R>& P,
                                            int tile_x, int tile_y, int chunk) {
-  using S = Sizes<R, TY, LEAN>;
+  constexpr bool LEAN = RK == 1;
+  using S = Sizes<R, TY, RK>;
   using T = Tile<TY, CPT>;
-  constexpr int DO = Rings<LEAN>::DO, DE = Rings<LEAN>::DE, NP = Rings<LEAN>::NP;
+  constexpr int DO = Rings<RK>::DO, DE = Rings<RK>::DE, NP = Rings<RK>::NP;
   constexpr int OH = T::OH, EH = T::EH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R* old = reinterpret_cast<R*>(smem_raw);
@@ -239,6 +278,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // fast-path sums as row-grouped trees in the plain variant (whatever the
   // kernel), in the reference's order in the B0 and absorbing-layer variants
   constexpr bool TREE = !B0 && !ABS;
+  // the plain FP32 variant's fast path: the two cells of a thread as float2
+  // pairs through the paired FP32 instructions
+  constexpr bool PK = FD && LEAN && CPT == 2;
   const R cc = P.cc, c1 = P.c1, c2 = P.c2, c3 = P.c3, ct = P.ct;
   const bool incr = P.incr != 0;
   R* const out0 = P.out0;
@@ -305,7 +347,21 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 
   // ---- per-thread constants --------------------------------------------------
   // update cells of this thread: (nxl, CPT * nq + r) of the NEW region, r < CPT
-  const int nxl = tid % T::TP, nq = tid / T::TP;
+  int nxl, nq;
+  if constexpr (T::WR) {
+    const int w = tid >> 5, l = tid & 31;
+    if (w < T::RG) {
+      nq = w;
+      nxl = l;
+    } else {  // the last warp: columns TX, TX+1 of every row group
+      const int e = (w - T::RG) * 32 + l;
+      nq = e >> 1;
+      nxl = TX + (e & 1);
+    }
+  } else {
+    nxl = tid % T::TP;
+    nq = tid / T::TP;
+  }
   const bool cell_thread = nxl < NX && nq < T::NY / CPT;
   const int gi = x0 - 1 + nxl, gj0 = y0 - 1 + CPT * nq;
   const bool out_x = gi < 0 || gi >= g.sx;
@@ -370,7 +426,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     const R* o0 = oth + so * (6 * S::OLDBOX);
     const R* o1 = oth + s1 * (6 * S::OLDBOX);
     const R* o2 = oth + s2 * (6 * S::OLDBOX);
-    const R* e1 = enth + (m & (DE - 1)) * (6 * S::ENBOX);
+    const R* e1 = enth + (m & (DE > 0 ? DE - 1 : 0)) * (6 * S::ENBOX);
     R* dst = nwth + (m & (DN - 1)) * (6 * S::NEWPL);
     // push + update (+ absorbing shell) of cell r from the OLD and EN rings.
     // Only shared-memory loads: the loads the CPT cells share are made once.
@@ -404,10 +460,30 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
                           !(mixed && (touch_per_xy || (per_z && (p < 0 || p >= g.sz))) &&
                             (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1))));
     if (all_push) {
+      if constexpr (PK) {
+        SmemOldPair<TY> a;
+        a.b[0] = reinterpret_cast<const float*>(o0);
+        a.b[1] = reinterpret_cast<const float*>(o1);
+        a.b[2] = reinterpret_cast<const float*>(o2);
+        float2 d[6];
+        push_pair_fast(a, (float)cc, d);
 #pragma unroll
-      for (int r = 0; r < CPT; ++r) {
-        push_update(r, v[r]);
-        frozen_cell[r] = false;
+        for (int c = 0; c < 6; ++c) {
+          const float2 f = a(c, 0, 0, 0);
+          float2 fn = f;
+          if constexpr (!STAGE1) fn = make_float2((float)en_nxt[0][c], (float)en_nxt[CPT - 1][c]);
+          const float2 w = combine2<C>((float)c1, (float)c2, (float)c3, fn, f, d[c], incr);
+          v[0][c] = (R)w.x;
+          v[CPT - 1][c] = (R)w.y;
+        }
+#pragma unroll
+        for (int r = 0; r < CPT; ++r) frozen_cell[r] = false;
+      } else {
+#pragma unroll
+        for (int r = 0; r < CPT; ++r) {
+          push_update(r, v[r]);
+          frozen_cell[r] = false;
+        }
       }
     } else {
 #pragma unroll
@@ -507,21 +583,38 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     const R* n2 = cth + ((m + 2) & (DN - 1)) * (6 * S::NEWPL);
     // all loads of the CPT cells first (they share neighbours), then the stores
     R v[CPT][6];
+    if constexpr (PK) {
+      SmemNewPair<TY> a;
+      a.b[0] = reinterpret_cast<const float*>(n0);
+      a.b[1] = reinterpret_cast<const float*>(n1);
+      a.b[2] = reinterpret_cast<const float*>(n2);
+      float2 e[3];
+      clean_pair_fast(a, e, 64.f * (float)ct);
 #pragma unroll
-    for (int r = 0; r < CPT; ++r) {
-      SmemNew<R, TY, LEAN> a;
-      a.b[0] = n0 + r * NP;
-      a.b[1] = n1 + r * NP;
-      a.b[2] = n2 + r * NP;
-      R e[3];
-      if constexpr (FD) clean_cell_fast<TREE>(a, e, ct);
-      else clean_cell<R, C, SmemNew<R, TY, LEAN>, false>(a, e, ct);
-      v[r][0] = e[0];
-      v[r][1] = e[1];
-      v[r][2] = e[2];
-      v[r][3] = a(BX, 0, 0, 0);
-      v[r][4] = a(BY, 0, 0, 0);
-      v[r][5] = a(BZ, 0, 0, 0);
+      for (int c = 0; c < 3; ++c) {
+        v[0][c] = (R)e[c].x;
+        v[CPT - 1][c] = (R)e[c].y;
+        const float2 b = a(BX + c, 0, 0, 0);
+        v[0][3 + c] = (R)b.x;
+        v[CPT - 1][3 + c] = (R)b.y;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < CPT; ++r) {
+        SmemNew<R, TY, RK> a;
+        a.b[0] = n0 + r * NP;
+        a.b[1] = n1 + r * NP;
+        a.b[2] = n2 + r * NP;
+        R e[3];
+        if constexpr (FD) clean_cell_fast<TREE>(a, e, ct);
+        else clean_cell<R, C, SmemNew<R, TY, RK>, false>(a, e, ct);
+        v[r][0] = e[0];
+        v[r][1] = e[1];
+        v[r][2] = e[2];
+        v[r][3] = a(BX, 0, 0, 0);
+        v[r][4] = a(BY, 0, 0, 0);
+        v[r][5] = a(BZ, 0, 0, 0);
+      }
     }
     const bool z_image = per_z && (k < NG || k >= g.sz - NG);
 #pragma unroll
@@ -593,18 +686,18 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // persistent block may initialise them again for its next work item.
   __syncthreads();
   if (tid == PRODUCER)
-    for (int s = 0; s < DO + DE; ++s) mbar_inval(smem_u32(bars + s));
+    for (int s = 0; s < S::BARS; ++s) mbar_inval(smem_u32(bars + s));
   return true;
 }
 
 #if !defined(FFE_BATCH_TY)
-// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk), tile height FUSED_TY.
-template <typename R, int C, bool B0, bool ABS, bool STAGE1>
-__global__ void __launch_bounds__(Tile<FUSED_TY, Cfg<R, B0, ABS>::CPT>::NT, Cfg<R, B0, ABS>::MINB)
+// One grid: block (x, y, z) = (tile_x, tile_y, z-chunk), tile height TY
+// (PLAIN_TY for the plain FP32 variant, FUSED_TY otherwise).
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY>
+__global__ void __launch_bounds__(Body<R, C, B0, ABS, TY>::NT, Body<R, C, B0, ABS, TY>::MINB)
     k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
-  using CF = Cfg<R, B0, ABS>;
-  stage_body<R, C, B0, ABS, STAGE1, FUSED_TY, CF::CPT, CF::LEAN>(maps.in, maps.en, P, blockIdx.x, blockIdx.y,
-                                                                 blockIdx.z);
+  using CF = Body<R, C, B0, ABS, TY>;
+  stage_body<R, C, B0, ABS, STAGE1, TY, CF::CPT, CF::RK>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 #else
 // Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
@@ -624,14 +717,14 @@ __global__ void __launch_bounds__(Tile<TY, BATCH_CPT>::NT, (sizeof(R) == 4 && TY
     bool ok;
     if (e.has_b0) {
       if (e.absorb)
-        ok = stage_body<R, C, true, true, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+        ok = stage_body<R, C, true, true, STAGE1, TY, BATCH_CPT, 0>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
       else
-        ok = stage_body<R, C, true, false, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+        ok = stage_body<R, C, true, false, STAGE1, TY, BATCH_CPT, 0>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     } else {
       if (e.absorb)
-        ok = stage_body<R, C, false, true, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+        ok = stage_body<R, C, false, true, STAGE1, TY, BATCH_CPT, 0>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
       else
-        ok = stage_body<R, C, false, false, STAGE1, TY, BATCH_CPT, false>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
+        ok = stage_body<R, C, false, false, STAGE1, TY, BATCH_CPT, 0>(e.mi, e.me, e.P, it.tx, it.ty, it.tz);
     }
     if (!ok) return;
   }
@@ -642,15 +735,15 @@ __global__ void __launch_bounds__(Tile<TY, BATCH_CPT>::NT, (sizeof(R) == 4 && TY
 // launch: the body of the single-grid kernel in its configuration for that
 // variant (Cfg), items and table as in k_fused_batch.
 template <typename R, int C, bool STAGE1, int TY, int VAR>
-__global__ void __launch_bounds__(Tile<TY, Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>::CPT>::NT,
-                                  Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>::MINB)
+__global__ void __launch_bounds__(Body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, TY>::NT,
+                                  Body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, TY>::MINB)
     k_fused_batch_var(const BatchItem* __restrict__ items, int nitems, const __grid_constant__ BoxTable<R> T) {
-  using CF = Cfg<R, (VAR & 2) != 0, (VAR & 1) != 0>;
+  using CF = Body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, TY>;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const BatchItem it = items[w];
     const BatchBox<R>& e = T.b[it.box];
-    if (!stage_body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, STAGE1, TY, CF::CPT, CF::LEAN>(e.mi, e.me, e.P, it.tx,
-                                                                                         it.ty, it.tz))
+    if (!stage_body<R, C, (VAR & 2) != 0, (VAR & 1) != 0, STAGE1, TY, CF::CPT, CF::RK>(e.mi, e.me, e.P, it.tx,
+                                                                                       it.ty, it.tz))
       return;
   }
 }
@@ -856,12 +949,16 @@ __global__ void k_uniform_ghosts_batch(const FixItem* __restrict__ items, const 
 
 template <typename R, int C>
 int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
-                    const void* maps_in, const void* maps_en, const CEB<R>& in_g, const CEB<R>& en_g,
-                    const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct, const UniformBC<R>* ub, int* err,
-                    cudaStream_t st) {
+                    const void* maps_in, const void* maps_en, const void* maps_plain, const CEB<R>& in_g,
+                    const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
+                    const UniformBC<R>* ub, int* err, cudaStream_t st) {
   using namespace FFE_FUSED_NS;
+  const bool abs = p.bnd[0] == 2;
+  // the plain FP32 variant takes the taller tile and its own stage-input maps
+  const bool plain = sizeof(R) == 4 && !has_b0 && !abs;
+  if (plain && !maps_plain) return -4;
   Maps M;
-  memcpy(M.in, maps_in, sizeof(M.in));
+  memcpy(M.in, plain ? maps_plain : maps_in, sizeof(M.in));
   memcpy(M.en, maps_en, sizeof(M.en));
   Params<R> P;
   P.g = g;
@@ -884,17 +981,18 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.err = err;
   P.ubc = ub ? 1 : 0;
   if (ub) P.ub = *ub;
-  constexpr int TY = FUSED_TY;
-  const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TY - 1) / TY;
-  const int kz = fused_planes_per_block(g, TY);
+  constexpr int TYP = sizeof(R) == 4 ? PLAIN_TY : FUSED_TY;
+  const int TYL = plain ? TYP : FUSED_TY;
+  const int tiles_x = (g.sx + TX - 1) / TX, tiles_y = (g.sy + TYL - 1) / TYL;
+  const int kz = fused_planes_per_block(g, TYL);
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
-  const bool abs = p.bnd[0] == 2;
   const bool s1 = stage == 1;
 #define FFE_GO(B0V, ABSV, S1V)                                                                   \
   do {                                                                                           \
-    auto kf = k_fused<R, C, B0V, ABSV, S1V>;                                                     \
-    const size_t smem = Sizes<R, TY, Cfg<R, B0V, ABSV>::LEAN>::BYTES;                            \
+    constexpr int TY = (!B0V && !ABSV) ? TYP : FUSED_TY;                                         \
+    auto kf = k_fused<R, C, B0V, ABSV, S1V, TY>;                                                 \
+    const size_t smem = Body<R, C, B0V, ABSV, TY>::SMEM;                                         \
     static bool attr_set = false;                                                                \
     if (!attr_set) {                                                                             \
       if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
@@ -904,7 +1002,7 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
         return -3;                                                                               \
       attr_set = true;                                                                           \
     }                                                                                            \
-    kf<<<grid, Tile<TY, Cfg<R, B0V, ABSV>::CPT>::NT, smem, st>>>(M, P);                          \
+    kf<<<grid, Body<R, C, B0V, ABSV, TY>::NT, smem, st>>>(M, P);                                 \
   } while (0)
   if (has_b0) {
     if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
@@ -985,8 +1083,8 @@ int fused_planes_per_block(const Geom& g, int ty) {
 }
 
 // Tensor maps of one array for the fused kernels of tile height ty: the OLD
-// box (tile + 2 halo) and the EN box (tile + 1 halo rows).  Coordinates:
-// (i + 2, j + 2, k + 2).
+// box (tile + 2 halo) and the EN box (tile + 1 halo rows; skipped when map_en
+// is null).  Coordinates: (i + 2, j + 2, k + 2).
 int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int es, int ty) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
@@ -1007,6 +1105,7 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
   CUresult r = encode((CUtensorMap*)map_old, dt, 3, base, dims, strides, box_old, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return -2;
+  if (!map_en) return 0;
   r = encode((CUtensorMap*)map_en, dt, 3, base, dims, strides, box_en, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -2;
@@ -1015,8 +1114,9 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
 
 #define FFE_INST_F(R, C)                                                                                        \
   template int FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,        \
-                                     const void*, const void*, const CEB<R>&, const CEB<R>&, const CEB<R>&,     \
-                                     bool, const EB<R>&, R, const UniformBC<R>*, int*, cudaStream_t);
+                                     const void*, const void*, const void*, const CEB<R>&, const CEB<R>&,       \
+                                     const CEB<R>&, bool, const EB<R>&, R, const UniformBC<R>*, int*,           \
+                                     cudaStream_t);
 #define FFE_INST_X(R, C)                                                                                        \
   template int FFE_FIX_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, const PsrBC<R>&, R, R, R, R, bool, \
                                   int, const CEB<R>&, const CEB<R>&, const CEB<R>&, bool, const EB<R>&, R, R*,   \
@@ -1042,23 +1142,23 @@ int launch_fused_batch_spec_t8(bool stage1, int var, const BatchItem* items, int
   constexpr int TY = FFE_BATCH_TY;
   if (nitems <= 0) return 0;
   if (var == 0) {
-    constexpr int NT = Tile<TY, Cfg<R, false, false>::CPT>::NT;
-    const size_t smem = Sizes<R, TY, Cfg<R, false, false>::LEAN>::BYTES;
+    constexpr int NT = Body<R, C, false, false, TY>::NT;
+    const size_t smem = Body<R, C, false, false, TY>::SMEM;
     if (stage1) k_fused_batch_var<R, C, true, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 0><<<grid, NT, smem, st>>>(items, nitems, T);
   } else if (var == 1) {
-    constexpr int NT = Tile<TY, Cfg<R, false, true>::CPT>::NT;
-    const size_t smem = Sizes<R, TY, Cfg<R, false, true>::LEAN>::BYTES;
+    constexpr int NT = Body<R, C, false, true, TY>::NT;
+    const size_t smem = Body<R, C, false, true, TY>::SMEM;
     if (stage1) k_fused_batch_var<R, C, true, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 1><<<grid, NT, smem, st>>>(items, nitems, T);
   } else if (var == 2) {
-    constexpr int NT = Tile<TY, Cfg<R, true, false>::CPT>::NT;
-    const size_t smem = Sizes<R, TY, Cfg<R, true, false>::LEAN>::BYTES;
+    constexpr int NT = Body<R, C, true, false, TY>::NT;
+    const size_t smem = Body<R, C, true, false, TY>::SMEM;
     if (stage1) k_fused_batch_var<R, C, true, TY, 2><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 2><<<grid, NT, smem, st>>>(items, nitems, T);
   } else if (var == 3) {
-    constexpr int NT = Tile<TY, Cfg<R, true, true>::CPT>::NT;
-    const size_t smem = Sizes<R, TY, Cfg<R, true, true>::LEAN>::BYTES;
+    constexpr int NT = Body<R, C, true, true, TY>::NT;
+    const size_t smem = Body<R, C, true, true, TY>::SMEM;
     if (stage1) k_fused_batch_var<R, C, true, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
     else k_fused_batch_var<R, C, false, TY, 3><<<grid, NT, smem, st>>>(items, nitems, T);
   } else {
@@ -1073,10 +1173,9 @@ template <typename R, int C>
 int fused_batch_prepare_spec_t8(int var) {
   using namespace FFE_FUSED_NS;
   constexpr int TY = FFE_BATCH_TY;
-  // only the plain variant takes the lean rings (Cfg)
-  const int NT = var == 0 ? Tile<TY, Cfg<R, false, false>::CPT>::NT : Tile<TY, Cfg<R, true, true>::CPT>::NT;
-  const size_t smem =
-      var == 0 ? Sizes<R, TY, Cfg<R, false, false>::LEAN>::BYTES : Sizes<R, TY, Cfg<R, true, true>::LEAN>::BYTES;
+  // only the plain variant takes the lean body (Body)
+  const int NT = var == 0 ? Body<R, C, false, false, TY>::NT : Body<R, C, true, true, TY>::NT;
+  const size_t smem = var == 0 ? Body<R, C, false, false, TY>::SMEM : Body<R, C, true, true, TY>::SMEM;
   void (*k1)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   void (*k2)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   if (var == 0) {

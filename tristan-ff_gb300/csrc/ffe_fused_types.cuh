@@ -10,6 +10,10 @@ namespace ffe {
 // width.  The tile height TY is a template parameter (8 or 16).
 constexpr int FUSED_TX = 32;
 constexpr int FUSED_TY = 8;  // tile height of the single-grid stage kernel
+// tile height of the single-grid stage kernel's plain FP32 variant (no B0, no
+// absorbing layer): its lean rings at this height still fit two blocks per SM
+// and the halo recompute falls from 1.33x (32 x 8 tile) to 1.24x (32 x 12)
+constexpr int PLAIN_TY = 12;
 
 struct Maps {  // one 3-D tensor map per component: stage input (OLD) and step start (EN)
   CUtensorMap in[6];

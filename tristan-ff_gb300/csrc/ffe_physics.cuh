@@ -373,4 +373,163 @@ __device__ __forceinline__ void clean_cell_fast(const A& a, float e[3], float ct
   }
 }
 
+// ---------------------------------------------------------------------------
+// Packed forms for two cells at once (FP32 fast path of the plain variant).
+// A thread that updates and cleans two cells stacked in y keeps each quantity
+// of both cells in one float2 (x: the lower cell, y: the upper) and evaluates
+// the same expressions with the paired FP32 instructions of sm_100+
+// (add/mul/fma.f32x2: one issue slot for two lanes' worth of work, each half
+// rounded exactly as its scalar instruction).  The accessor returns
+// float2 {value at the lower cell, value at the upper cell}.  Quotients and
+// square roots have no paired form and run per half.  The four- and
+// eight-term sums are added as balanced trees grouped by z plane.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as fma(b, -1, a): the product is exact, so it rounds as a - b does
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2s(float s) { return make_float2(s, s); }
+// hardware reciprocal approximation (PTX rcp.approx.ftz.f32), per half
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float2 f2rcp(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
+// -1 / x per half
+__device__ __forceinline__ float2 f2nrcp(float2 a) { return make_float2(rcp_approx(-a.x), rcp_approx(-a.y)); }
+
+template <class A>
+__device__ __forceinline__ float2 rho2(const A& a, int di, int dj, int dk) {
+  return f2add(f2add(f2sub(a(EX, di, dj, dk), a(EX, di - 1, dj, dk)), f2sub(a(EY, di, dj, dk), a(EY, di, dj - 1, dk))),
+               f2sub(a(EZ, di, dj, dk), a(EZ, di, dj, dk - 1)));
+}
+// F(0,dj,dk) + F(dx,dj,dk)
+template <class A>
+__device__ __forceinline__ float2 xpair2(const A& a, int c, int dx, int dj, int dk) {
+  return f2add(a(c, 0, dj, dk), a(c, dx, dj, dk));
+}
+
+struct PointSums2 {
+  float2 sa, sb, s8, s2a, s2b;
+};
+// the bare sums at the Ex, Ey, Ez points (the same neighbours as sums_x/y/z)
+template <class A>
+__device__ __forceinline__ PointSums2 sums2_x(const A& a) {
+  PointSums2 s;
+  s.s2a = f2add(a(BY, 0, 0, 0), a(BY, 0, 0, -1));
+  s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, 0, -1, 0));
+  s.sa = f2add(xpair2(a, EY, 1, 0, 0), xpair2(a, EY, 1, -1, 0));
+  s.sb = f2add(xpair2(a, EZ, 1, 0, 0), xpair2(a, EZ, 1, 0, -1));
+  s.s8 = f2add(f2add(xpair2(a, BX, 1, 0, 0), xpair2(a, BX, 1, -1, 0)),
+               f2add(xpair2(a, BX, 1, 0, -1), xpair2(a, BX, 1, -1, -1)));
+  return s;
+}
+template <class A>
+__device__ __forceinline__ PointSums2 sums2_y(const A& a) {
+  PointSums2 s;
+  s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, 0, -1));
+  s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, -1, 0, 0));
+  s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 1, 0));
+  s.sb = f2add(f2add(a(EZ, 0, 0, 0), a(EZ, 0, 1, 0)), f2add(a(EZ, 0, 0, -1), a(EZ, 0, 1, -1)));
+  s.s8 = f2add(f2add(xpair2(a, BY, -1, 0, 0), xpair2(a, BY, -1, 1, 0)),
+               f2add(xpair2(a, BY, -1, 0, -1), xpair2(a, BY, -1, 1, -1)));
+  return s;
+}
+template <class A>
+__device__ __forceinline__ PointSums2 sums2_z(const A& a) {
+  PointSums2 s;
+  s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, -1, 0));
+  s.s2b = f2add(a(BY, 0, 0, 0), a(BY, -1, 0, 0));
+  s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 0, 1));
+  s.sb = f2add(f2add(a(EY, 0, 0, 0), a(EY, 0, -1, 0)), f2add(a(EY, 0, 0, 1), a(EY, 0, -1, 1)));
+  s.s8 = f2add(f2add(xpair2(a, BZ, -1, 0, 0), xpair2(a, BZ, -1, -1, 0)),
+               f2add(xpair2(a, BZ, -1, 0, 1), xpair2(a, BZ, -1, -1, 1)));
+  return s;
+}
+
+// 64 B^2 of a point from its bare sums
+__device__ __forceinline__ float2 bmag64_2(const PointSums2& s) {
+  return f2fma(s.s8, s.s8, f2mul(f2s(16.f), f2fma(s.s2a, s.s2a, f2mul(s.s2b, s.s2b))));
+}
+
+// The current factor k = 4 CC Srho / (64 B^2 + 64 TINY) of a point and its
+// limited transverse E sums (ea, eb).  The limiter factor is min(1,
+// sqrt(B^2 / E^2)): 1 where E^2 <= B^2 (and where E = 0), the reference's
+// sqrt(B^2/E^2) where E^2 > B^2.
+__device__ __forceinline__ float2 fast_current2(float cc4, float t64, float2 sr, float2 e0, const PointSums2& s,
+                                                float2& ea, float2& eb) {
+  const float2 bm = bmag64_2(s);
+  const float2 em = f2fma(f2mul(f2s(64.f), e0), e0, f2mul(f2s(4.f), f2fma(s.sa, s.sa, f2mul(s.sb, s.sb))));
+  const float2 q = f2mul(bm, f2rcp(em));
+  const float2 corr = make_float2(fminf(1.f, sqrt_approx(q.x)), fminf(1.f, sqrt_approx(q.y)));
+  ea = f2mul(s.sa, corr);
+  eb = f2mul(s.sb, corr);
+  return f2mul(f2mul(f2s(cc4), sr), f2rcp(f2add(bm, f2s(t64))));
+}
+
+// push_cell_fast (no B0) for two cells
+template <class A>
+__device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]) {
+  const float2 ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
+  const float2 bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
+  const float2 c2 = f2s(cc);
+  d[3] = f2mul(c2, f2sub(f2sub(a(EY, 0, 0, 1), ey0), f2sub(a(EZ, 0, 1, 0), ez0)));
+  d[4] = f2mul(c2, f2sub(f2sub(a(EZ, 1, 0, 0), ez0), f2sub(a(EX, 0, 0, 1), ex0)));
+  d[5] = f2mul(c2, f2sub(f2sub(a(EX, 0, 1, 0), ex0), f2sub(a(EY, 1, 0, 0), ey0)));
+  const float2 mcc = f2s(-cc);  // -(CC*X) == (-CC)*X exactly
+  const float2 cbx = f2mul(mcc, f2sub(f2sub(by0, a(BY, 0, 0, -1)), f2sub(bz0, a(BZ, 0, -1, 0))));
+  const float2 cby = f2mul(mcc, f2sub(f2sub(bz0, a(BZ, -1, 0, 0)), f2sub(bx0, a(BX, 0, 0, -1))));
+  const float2 cbz = f2mul(mcc, f2sub(f2sub(bx0, a(BX, 0, -1, 0)), f2sub(by0, a(BY, -1, 0, 0))));
+  const float2 r0 = rho2(a, 0, 0, 0);
+  const float cc4 = 4.f * cc, t64 = 64.f * tiny<float>();
+  float2 ea, eb, k;
+  {  // X current at the Ex point (field_solver.F90:91-111): dE_x = -CC curl - k (ea s2b - s2a eb)
+    const PointSums2 s = sums2_x(a);
+    k = fast_current2(cc4, t64, f2add(rho2(a, 1, 0, 0), r0), ex0, s, ea, eb);
+    d[0] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbx);
+  }
+  {  // Y current at the Ey point (:114-134): - k (eb s2a - ea s2b)
+    const PointSums2 s = sums2_y(a);
+    k = fast_current2(cc4, t64, f2add(rho2(a, 0, 1, 0), r0), ey0, s, ea, eb);
+    d[1] = f2fma(k, f2sub(f2mul(ea, s.s2b), f2mul(eb, s.s2a)), cby);
+  }
+  {  // Z current at the Ez point (:137-157): - k (ea s2b - s2a eb)
+    const PointSums2 s = sums2_z(a);
+    k = fast_current2(cc4, t64, f2add(r0, rho2(a, 0, 0, 1)), ez0, s, ea, eb);
+    d[2] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbz);
+  }
+}
+
+// clean_cell_fast for two cells (ct64 = 64 x the cleaning's TINY, 0 by default):
+// E_i - (E.B-sums) S8 / (64 B^2 + ct64)
+template <class A>
+__device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float ct64) {
+  const float2 ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
+  const float2 c64 = f2s(ct64);
+  {  // Ex point (:289-300)
+    const PointSums2 s = sums2_x(a);
+    const float2 ep = f2fma(ex0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
+    e[0] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ex0);
+  }
+  {  // Ey point (:303-314)
+    const PointSums2 s = sums2_y(a);
+    const float2 ep = f2fma(ey0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
+    e[1] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ey0);
+  }
+  {  // Ez point (:317-328)
+    const PointSums2 s = sums2_z(a);
+    const float2 ep = f2fma(ez0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
+    e[2] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ez0);
+  }
+}
+
+// RK combination for two cells (see combine)
+template <int C>
+__device__ __forceinline__ float2 combine2(float c1, float c2, float c3, float2 fn, float2 f, float2 df, bool incr) {
+  if (C && incr) return f2add(fn, f2fma(f2s(c2), f2sub(f, fn), f2mul(f2s(c3), df)));
+  return f2fma(f2s(c3), df, f2fma(f2s(c1), fn, f2mul(f2s(c2), f)));
+}
+
 }  // namespace ffe
