@@ -70,10 +70,13 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="edge of the CPU sample grid (0 = auto)")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing: run FP64, FP32 and FP32C for N steps and report their errors")
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "serve", "psr-accuracy"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "serve", "psr", "psr-accuracy"],
                     help="grid: the single 512^3 grid (default line); batch: 64 uneven boxes, batched vs "
                          "one grid at a time; serve: a Poisson stream of pulsar runs, continuous batching "
-                         "vs one grid at a time")
+                         "vs one grid at a time; psr: the 512^3 pulsar magnetosphere (rate and error vs FP64)")
+    ap.add_argument("--batch-steps", type=int, default=500, help="batch: steps of every box")
+    ap.add_argument("--psr-marks", default="50,100,200,400",
+                    help="psr: step counts at which the error against FP64 is stated")
     ap.add_argument("--batch-boxes", type=int, default=64)
     ap.add_argument("--batch-kind", default="mixed", choices=["mixed", "packet"],
                     help="batch: half packets and half flux tubes (which carry a B0 field), or packets only")
@@ -449,7 +452,7 @@ def bench_batch(args):
     prec = ffe.PRECISIONS[args.precision]
     specs = workloads.batch_boxes(args.batch_boxes, kind=args.batch_kind)
     cells = [s["size"][0] * s["size"][1] * s["size"][2] for s in specs]
-    K = args.steps
+    K = args.batch_steps
     # one grid at a time: each box runs all K steps, then the next box
     seq = [workloads.build_solver(sp, prec) for sp in specs]
     for g in seq:
@@ -495,8 +498,10 @@ def bench_batch(args):
         "unit": "cell-updates/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
         "higher_is_better": True, "dtype": args.precision, "data": "synthetic",
         "one_grid_at_a_time": total / t_seq, "speedup_vs_one_at_a_time": t_seq / t_bat,
-        "time_to_result_s": {"batched": {"p50": t_bat, "p99": t_bat},
-                             "one_at_a_time": {"p50": pct(done, 50), "p99": pct(done, 99)}},
+        "time_to_result_s": {"batched_all_boxes": t_bat,
+                             "one_at_a_time": {"p50": pct(done, 50), "p99": pct(done, 99), "last": t_seq},
+                             "note": "the batch advances every box in one call, so all its results arrive "
+                                     "together; one at a time, box i's result arrives after boxes 0..i"},
         "max_rel_l2_batched_vs_single": diff, "tiling": tiling, "autotune_ms_per_stage": tune_ms,
         "gpu_launches": launches * K,
         "config": {"workload": "%d boxes, sides U[48,160], %s"
@@ -505,6 +510,87 @@ def bench_batch(args):
                    "cells": int(sum(cells)),
                    "timing": "host clock around synchronised runs (includes launch overhead of both paths)"},
     }))
+
+
+def bench_psr(args):
+    """The pulsar magnetosphere at --size^3 (512^3): user_psr with a rotating
+    conducting sphere of radius 24 cells at the centre, inclination 30
+    degrees, light cylinder at 120 cells (period 2 pi 120 / c steps), the
+    dipole scaled to B = 1e3 at the stellar surface, an absorbing shell 48
+    cells thick (user/user_psr.F90:72-383, src/algorithms/field_solver.F90:
+    198-268).  The reference's shell (jg = i + y0, clamped, TINY in the
+    cleaning) and the true-y shell, one line each: the step rate of FP32C and
+    of FP32CD (B^2 denominators in double) with the roofline at 54 words per
+    cell-update, and their relative L2 / L-infinity error of E and B against
+    the FP64 path at the step counts of --psr-marks."""
+    import math
+    import torch
+    import ffe
+    import build as ffe_build
+    torch.cuda.set_device(0)
+    ffe_build.build()
+    S = args.size
+    cc = 0.45
+    params = (24.0 * S / 512, 30.0, 2.0 * math.pi * (120.0 * S / 512) / cc, 1000.0)
+    buff = int(round(48 * S / 512))
+    marks = [int(m) for m in args.psr_marks.split(",") if m]
+    peak, peak_kind = peaks()
+    names = ("ex", "ey", "ez", "bx", "by", "bz")
+    base = ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY
+    stream = torch.cuda.Stream()
+
+    def make(prec, flags):
+        d = ffe.make_desc((S,) * 3, precision=prec, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff, cc=cc,
+                          setup=ffe.SETUP_PSR, params=params, flags=flags, stream=stream.cuda_stream)
+        g = ffe.Solver(d)
+        g.userInitialize()
+        g.mainloop_prologue()
+        return g
+
+    for label, flags in (("reference shell (jg = i + y0), clamped", base),
+                         ("true-y shell, clamped", base | ffe.FLAG_ABSORB_TRUE_Y)):
+        rates = {}
+        for pn in ("fp32c", "fp32cd"):
+            g = make(ffe.PRECISIONS[pn], flags)
+            g.mainloop(args.warmup, 0)
+            g.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            k = args.steps if pn == "fp32c" else max(2, args.steps // 5)
+            e0.record(stream)
+            g.mainloop(k, args.warmup)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / k
+            ach = S ** 3 * WORDS_PER_CELL_STEP * 4 / (ms / 1e3) / 1e9
+            rates[pn] = {"value": S ** 3 / (ms / 1e3), "ms_per_step": ms, "steps": k,
+                         "roofline_frac": ach / peak, "finite": g.check_finite()}
+            g.close()
+        runs = {pn: make(ffe.PRECISIONS[pn], flags) for pn in ("fp64", "fp32c", "fp32cd")}
+        errs, done = [], 0
+        t0 = time.perf_counter()
+        for m in marks:
+            for g in runs.values():
+                g.mainloop(m - done, done)
+            done = m
+            ref = {n: ffe.interior(a) for n, a in runs["fp64"].fields().items()}
+            row = {"step": m}
+            for pn in ("fp32c", "fp32cd"):
+                row[pn] = rel_errors({n: ffe.interior(a) for n, a in runs[pn].fields().items()}, ref)
+            errs.append(row)
+        for g in runs.values():
+            g.close()
+        print(json.dumps({
+            "metric": "cell-updates/s per RK3 step, pulsar magnetosphere", "value": rates["fp32c"]["value"],
+            "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": rates["fp32c"]["ms_per_step"], "higher_is_better": True, "dtype": "fp32c",
+            "data": "synthetic", "shell": label, "rates": rates,
+            "roofline": {"bound": "hbm", "peak": peak, "unit": "GB/s", "words_per_cell_update": WORDS_PER_CELL_STEP,
+                         "peak_source": peak_kind},
+            "error_vs_fp64": errs, "error_seconds": time.perf_counter() - t0,
+            "config": {"workload": "pulsar magnetosphere %d^3" % S, "psr_radius": params[0],
+                       "inclination_deg": 30.0, "light_cylinder": 120.0 * S / 512, "period_steps": params[2],
+                       "surface_b": 1000.0, "absorb_buff": buff, "cc": cc,
+                       "stopped_at_step": marks[-1] if marks else 0}}), flush=True)
 
 
 def psr_accuracy(args):
@@ -636,6 +722,9 @@ def main():
         return
     if args.workload == "psr-accuracy":
         psr_accuracy(args)
+        return
+    if args.workload == "psr":
+        bench_psr(args)
         return
     if args.workload == "serve":
         if args.precision == "fp32":

@@ -141,6 +141,14 @@ typedef enum {
    numerically unstable: two FP64 builds that differ only in rounding drift
    apart by 10% (relative L2 of E) within 200 steps.                       */
 #define FFE_FLAG_ABSORB_TRUE_Y 4
+/* For failure-detection tests only (no counterpart in the reference): in
+   every block of the fused stage kernels the thread that issues the TMA plane
+   copies leaves out one plane's copy, and the blocks give up waiting for it
+   after about 2^14 probes instead of 2^22.  The waits run out, the blocks set
+   the error word and return, and the next ffe_synchronize (or
+   ffe_batch_synchronize) returns FFE_ETIMEOUT; the CUDA context stays usable.
+   Results of a handle with this flag are meaningless.                      */
+#define FFE_FLAG_TEST_WITHHOLD_COPY 8
 
 typedef struct {
   int32_t sx, sy, sz;          /* interior cells of this meshblock           */

@@ -77,3 +77,16 @@ def test_served_matches_plain_path_and_fp64(served):
     g.synchronize()
     assert eb_err(g.fields(), r.result) <= 1e-5
     g.close()
+
+
+def test_served_runs_match_the_oracle(served, oracle_mod):
+    """The two smallest served runs against the CPU oracle (FP32C, the same
+    arithmetic with exact quotients and no contraction) after their full step
+    counts: the served fast path stays within 2e-5 relative L2."""
+    reqs, srv, recs = served
+    for r in sorted(recs, key=lambda x: x.cells * x.steps)[:2]:
+        o = workloads.init_run(oracle_mod.Oracle(workloads.run_desc(r.spec, ffe.FP32C)), r.spec)
+        o.mainloop(r.steps, 0)
+        err = eb_err(o.fields(), r.result)
+        o.close()
+        assert err <= 2e-5, (r.id, r.steps, err)

@@ -8,6 +8,9 @@ from ffe import serve, workloads
 
 
 class FakeSolver:
+    def check_finite(self):
+        return True
+
     def __init__(self, spec):
         self.spec = spec
         self.steps_run = 0
@@ -92,12 +95,9 @@ def test_shortest_job_first_admits_small_runs_first():
 def test_oversized_request_is_refused():
     q = requests(1)
     srv = serve.Server(hbm_budget=1000.0, build=lambda s, p: FakeSolver(s), batch_cls=FakeBatch)
-    try:
-        srv.serve(q)
-    except ffe.FFEError as e:
-        assert e.status == -1
-    else:
-        raise AssertionError("expected a refusal")
+    (r,) = srv.serve(q)
+    assert r.status == "rejected" and r.result is None and "budget" in r.error
+    assert srv.epochs == 0
 
 
 def test_served_workload_is_seeded():
@@ -121,3 +121,40 @@ def test_cell_cap_limits_concurrency():
     srv = serve.Server(hbm_budget=1e15, max_active_cells=1, build=lambda s, p: FakeSolver(s), batch_cls=FakeBatch)
     recs = srv.serve(reqs[:3])
     assert all(n == 1 for n, _, _, _ in srv.log) and all(r.finished is not None for r in recs)
+
+
+class FakeFiniteSolver(FakeSolver):
+    """A stand-in whose fields turn non-finite (a NaN injected on the host)."""
+
+    def __init__(self, spec, bad):
+        super().__init__(spec)
+        self.bad = bad
+
+    def check_finite(self):
+        return not self.bad
+
+
+def test_failures_stay_with_their_run():
+    """An oversized request is rejected alone, a malformed one too, and a run
+    whose fields are not finite at the end is marked failed; the reference
+    stops the whole job instead (src/tools/error_handling.F90:8-13)."""
+    reqs = requests(n=10, rate=1e6)
+    sizes = [serve._desc_bytes(q, ffe.FP32C) for q in reqs]
+    budget = 2.5 * max(sizes)
+    big = {"kind": "psr", "size": (4096,) * 3, "incl": 10.0, "steps": 5, "arrival": 0.0, "id": "big"}
+    bad_kind = {"kind": "nonsense", "size": (16,) * 3, "steps": 5, "arrival": 0.0, "id": "bad-kind"}
+    poisoned = reqs[3]["id"]
+    srv = serve.Server(precision=ffe.FP32C, hbm_budget=budget, epoch_steps=16, keep_results=True,
+                       build=lambda spec, prec: FakeFiniteSolver(spec, spec["id"] == poisoned),
+                       batch_cls=FakeBatch)
+    recs = srv.serve(reqs + [big, bad_kind])
+    by_id = {r.id: r for r in recs}
+    assert by_id["big"].status == "rejected" and "budget" in by_id["big"].error
+    assert by_id["bad-kind"].status == "rejected"
+    assert by_id[poisoned].status == "failed" and by_id[poisoned].result is None
+    for q in reqs:
+        if q["id"] != poisoned:
+            r = by_id[q["id"]]
+            assert r.status == "ok" and r.result == {"steps": r.steps}
+    rep = serve.report(recs)
+    assert (rep["completed"], rep["rejected"], rep["failed"]) == (len(reqs) - 1, 2, 1)

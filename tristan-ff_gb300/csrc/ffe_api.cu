@@ -526,7 +526,9 @@ int validate_desc(ffe_grid_desc& d) {
     return set_thread_err(FFE_EINVAL, "bad precision %d", d.precision);
   if (d.setup < FFE_SETUP_NONE || d.setup > FFE_SETUP_LOOP) return set_thread_err(FFE_EINVAL, "bad setup %d", d.setup);
   if (d.path < FFE_PATH_AUTO || d.path > FFE_PATH_FUSED_EXACT) return set_thread_err(FFE_EINVAL, "bad path %d", d.path);
-  if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY | FFE_FLAG_ABSORB_TRUE_Y)) || d.reserved)
+  if ((d.flags & ~(FFE_FLAG_ABSORB_CLAMP | FFE_FLAG_CLEAN_TINY | FFE_FLAG_ABSORB_TRUE_Y |
+                   FFE_FLAG_TEST_WITHHOLD_COPY)) ||
+      d.reserved)
     return set_thread_err(FFE_EINVAL, "unknown flags 0x%x", d.flags);
   for (int a = 0; a < 3; ++a)
     if (d.boundary[a] < 0 || d.boundary[a] > 2) return set_thread_err(FFE_EINVAL, "bad boundary %d", d.boundary[a]);
@@ -572,6 +574,7 @@ size_t plan_arena(ffe_solver* h, size_t* abytes, size_t* pbytes) {
   p.gsx = d.gsx; p.gsy = d.gsy; p.gsz = d.gsz;
   for (int a = 0; a < 3; ++a) p.bnd[a] = d.boundary[a];
   p.absorb_buff = d.absorb_buff;
+  p.withhold_copy = (d.flags & FFE_FLAG_TEST_WITHHOLD_COPY) ? 1 : 0;
   p.cc = d.cc;
   *abytes = ((size_t)g.nelem * h->es + 255) / 256 * 256;
   size_t total = *abytes * 22;

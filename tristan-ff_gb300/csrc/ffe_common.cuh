@@ -43,6 +43,7 @@ struct Phys {
   int gsx, gsy, gsz;   // global mesh
   int bnd[3];          // 0 open, 1 periodic, 2 absorbing
   int absorb_buff;
+  int withhold_copy;   // FFE_FLAG_TEST_WITHHOLD_COPY (failure-detection tests only)
   double cc;
 };
 

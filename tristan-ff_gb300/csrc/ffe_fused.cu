@@ -42,6 +42,7 @@
 // grids all share one B0 / absorbing-layer variant (k_fused_batch_var).
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <climits>
 #include <cstring>
 #include "ffe_kernels.h"
 #include "ffe_fused_types.cuh"
@@ -73,6 +74,8 @@ constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+T
 constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
 constexpr int DN = 4;                    // NEW ring depth
 constexpr long long WAIT_LIMIT = 1LL << 22;
+// probes of a wait when the test flag withholds a copy (FFE_FLAG_TEST_WITHHOLD_COPY)
+constexpr long long TEST_WAIT_LIMIT = 1LL << 14;
 
 // Tile of height TY: OLD boxes of OH rows (y0-2 .. y0+TY+1), EN boxes of EH
 // rows (y0-1 .. y0+TY), NEW planes of NY rows; OLD and EN rows are OW words,
@@ -190,10 +193,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: true when the phase completed (one probe in the common case)
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+// bounded wait: true when the phase completed (one probe in the common
+// case), false after `limit` probes
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit = WAIT_LIMIT) {
   if (__builtin_expect(mbar_try_wait(bar, parity), 1)) return true;
-  for (long long it = 1; it < WAIT_LIMIT; ++it)
+  for (long long it = 1; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -292,7 +296,12 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // OLD plane p lives in slot (p - kb + 2) % DO, EN plane p in (p - kb + 1) % DE.
   int old_next = kb - 2, en_next = kb - 1;
   const int old_last = ke + 1, en_last = ke;
+  // failure-detection test: the copy of OLD plane kb+1 is left out, so the
+  // wait for it runs out after TEST_WAIT_LIMIT probes
+  const int withheld = P.p.withhold_copy ? kb + 1 : INT_MIN;
+  const long long wlim = P.p.withhold_copy ? TEST_WAIT_LIMIT : WAIT_LIMIT;
   auto issue_old = [&](int p) {
+    if (p == withheld) return;
     const int s = (p - kb + 2) % DO;
     const unsigned bar = bar_old + 8 * s;
     mbar_expect_tx(bar, 6u * OW * OH * sizeof(R));
@@ -334,13 +343,13 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   unsigned ow_par = 0;     // its phase parity
   int ew = 0;              // EN planes waited so far (kb-1 first)
   auto wait_old = [&]() {
-    const bool ok = mbar_wait(bar_old + 8 * ow_slot, ow_par);
+    const bool ok = mbar_wait(bar_old + 8 * ow_slot, ow_par, wlim);
     if (++ow_slot == DO) { ow_slot = 0; ow_par ^= 1u; }
     return ok;
   };
   auto wait_en = [&]() {
     if (STAGE1 || DE == 0) return true;
-    const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1));
+    const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1), wlim);
     ++ew;
     return ok;
   };
@@ -674,10 +683,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       atomicExch(P.err, 1);
       // drain the copies that may still be in flight: the last use of each slot
       for (int p = max(kb - 2, old_next - DO); p < old_next; ++p)
-        mbar_wait(bar_old + 8 * ((p - kb + 2) % DO), (unsigned)(((p - kb + 2) / DO) & 1));
+        if (p != withheld) mbar_wait(bar_old + 8 * ((p - kb + 2) % DO), (unsigned)(((p - kb + 2) / DO) & 1), wlim);
       if constexpr (!STAGE1 && DE > 0)
         for (int p = max(kb - 1, en_next - DE); p < en_next; ++p)
-          mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1));
+          mbar_wait(bar_en + 8 * ((p - kb + 1) % DE), (unsigned)(((p - kb + 1) / DE) & 1), wlim);
     }
     __syncthreads();
     return false;

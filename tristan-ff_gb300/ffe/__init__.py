@@ -39,6 +39,7 @@ PATH_AUTO, PATH_STAGED, PATH_FUSED, PATH_FUSED_EXACT = 0, 1, 2, 3
 FLAG_ABSORB_CLAMP = 1
 FLAG_CLEAN_TINY = 2
 FLAG_ABSORB_TRUE_Y = 4
+FLAG_TEST_WITHHOLD_COPY = 8  # failure-detection tests only (include/ffe.h)
 FIELDS = ("ex", "ey", "ez", "bx", "by", "bz", "b0x", "b0y", "b0z",
           "dex", "dey", "dez", "dbx", "dby", "dbz",
           "enx", "eny", "enz", "bnx", "bny", "bnz", "rho")

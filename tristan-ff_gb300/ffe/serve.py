@@ -19,6 +19,12 @@ run alone on the single-grid fused path, in arrival order.
 
 Time-to-result of a request = from its arrival to the moment its result is
 on the host.  Times are wall-clock seconds from the start of serving.
+
+Failures stay with their run.  The reference stops the whole job on an error
+(src/tools/error_handling.F90:8-13); here a request that cannot fit the HBM
+budget is rejected alone (status "rejected"), and a run whose fields are no
+longer finite when it finishes (ffe_check_finite) is marked "failed" with
+no result; every other run goes on and finishes as it would have alone.
 """
 import time
 
@@ -30,7 +36,7 @@ from ffe import workloads
 
 class Record:
     __slots__ = ("id", "spec", "steps", "done", "solver", "bytes", "arrival", "admitted", "finished", "cells",
-                 "result")
+                 "result", "status", "error")
 
     def __init__(self, spec):
         self.id = spec.get("id")
@@ -45,37 +51,42 @@ class Record:
         s = spec["size"]
         self.cells = int(s[0]) * int(s[1]) * int(s[2])
         self.result = None
+        self.status = "queued"   # then "ok", "rejected" or "failed"
+        self.error = None
 
     def summary(self):
         return {"id": self.id, "size": list(self.spec["size"]), "steps": self.steps, "arrival": self.arrival,
-                "admitted": self.admitted, "finished": self.finished,
+                "admitted": self.admitted, "finished": self.finished, "status": self.status, "error": self.error,
                 "time_to_result": None if self.finished is None else self.finished - self.arrival}
 
 
 def _desc_bytes(spec, precision):
     """Device bytes of a run, from the descriptor build_solver would use."""
-    size = tuple(spec["size"])
-    if spec["kind"] == "psr":
-        side = size[0]
-        buff = spec.get("absorb_buff", int(np.ceil(side * 48 / 512)))
-        d = ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
-                          setup=ffe.SETUP_PSR, params=workloads.psr_params(side, spec["incl"]))
-    elif spec["kind"] == "tube":
-        d = ffe.make_desc(size, precision=precision, boundary=(ffe.PERIODIC, ffe.PERIODIC, ffe.OPEN),
-                          setup=ffe.SETUP_UNIFORM, params=workloads.tube_params(size, spec["beta"]))
-    else:
-        d = ffe.make_desc(size, precision=precision)
-    return ffe.desc_device_bytes(d)
+    return ffe.desc_device_bytes(workloads.run_desc(spec, precision))
 
 
 def _finish(r, now, keep):
-    """Copy the run's E, B to the host (kept when `keep` is true or holds the
-    run's id), record the time, free the run's device memory."""
-    fields = r.solver.fields()
-    r.result = fields if (keep is True or (keep and r.id in keep)) else None
+    """Check that the run's fields are finite, copy its E, B to the host (kept
+    when `keep` is true or holds the run's id), record the time, free the
+    run's device memory.  A run with NaN or Inf in E or B is marked failed and
+    gives no result."""
+    if r.solver.check_finite():
+        fields = r.solver.fields()
+        r.result = fields if (keep is True or (keep and r.id in keep)) else None
+        r.status = "ok"
+    else:
+        r.result = None
+        r.status = "failed"
+        r.error = "non-finite E or B after %d steps" % r.done
     r.finished = now()
     r.solver.close()
     r.solver = None
+
+
+def _reject(r, budget, now):
+    r.status = "rejected"
+    r.error = "needs %d device bytes, more than the budget of %d" % (r.bytes, int(budget))
+    r.finished = now()
 
 
 class Server:
@@ -107,13 +118,14 @@ class Server:
 
     def serve(self, requests):
         recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
-        for r in recs:
-            r.bytes = _desc_bytes(r.spec, self.precision)
-            if r.bytes > self.budget:
-                raise ffe.FFEError("request %s needs %d bytes, more than the budget" % (r.id, r.bytes), -1)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
-        pending = list(recs)
+        for r in recs:
+            try:
+                r.bytes = _desc_bytes(r.spec, self.precision)
+            except (ffe.FFEError, ValueError, KeyError) as e:  # a malformed request fails alone
+                r.status, r.error, r.finished = "rejected", str(e), now()
+        pending = [r for r in recs if r.status == "queued"]
         queue, active = [], []
         used = 0
         cells = 0
@@ -122,7 +134,11 @@ class Server:
         while pending or queue or active or leaving:
             t = now()
             while pending and pending[0].arrival <= t:
-                queue.append(pending.pop(0))
+                r = pending.pop(0)
+                if r.bytes > self.budget:  # can never fit: rejected alone
+                    _reject(r, self.budget, now)
+                else:
+                    queue.append(r)
             if self.policy == "sjf":  # least work (cells x steps) first among the waiting
                 queue.sort(key=lambda r: (r.cells * r.steps, r.arrival))
             while queue and used + queue[0].bytes <= self.budget and (
@@ -194,13 +210,19 @@ def serve_plain(requests, precision=ffe.FP32C, keep_results=False, policy="fifo"
 
 
 def report(recs):
-    """Aggregate throughput (cell-updates over the span from the first arrival
-    to the last result) and time-to-result percentiles."""
-    ttr = np.array([r.finished - r.arrival for r in recs])
-    first = min(r.arrival for r in recs)
-    last = max(r.finished for r in recs)
-    work = float(sum(r.cells * r.steps for r in recs))
-    return {"requests": len(recs), "cell_updates": work, "span_s": last - first,
-            "cell_updates_per_s": work / (last - first),
-            "time_to_result_s": {"p50": float(np.percentile(ttr, 50)), "p99": float(np.percentile(ttr, 99)),
-                                 "max": float(ttr.max())}}
+    """Aggregate throughput (cell-updates of the completed runs over the span
+    from the first arrival to the last result), time-to-result percentiles of
+    the completed runs, and how many requests were rejected or failed."""
+    ok = [r for r in recs if r.status == "ok"]
+    out = {"requests": len(recs), "completed": len(ok),
+           "rejected": sum(r.status == "rejected" for r in recs), "failed": sum(r.status == "failed" for r in recs)}
+    if not ok:
+        return out
+    ttr = np.array([r.finished - r.arrival for r in ok])
+    first = min(r.arrival for r in ok)
+    last = max(r.finished for r in ok)
+    work = float(sum(r.cells * r.steps for r in ok))
+    out.update({"cell_updates": work, "span_s": last - first, "cell_updates_per_s": work / (last - first),
+                "time_to_result_s": {"p50": float(np.percentile(ttr, 50)), "p99": float(np.percentile(ttr, 99)),
+                                     "max": float(ttr.max())}})
+    return out

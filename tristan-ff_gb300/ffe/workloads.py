@@ -142,36 +142,43 @@ def served_requests(n, seed=4, rate=20.0, lo=96, hi=256, steps=(200, 2000), shel
     return out
 
 
-def build_solver(spec, precision, path=None, lib_path=None):
-    """A Solver for a run spec, initialised and past the main-loop prologue.
-    Pulsar runs use the clamped absorbing shell with TINY in the cleaning, and
-    the true-y shell when spec["shell"] == "true_y"."""
+def run_desc(spec, precision, path=None):
+    """The descriptor of a run spec.  Pulsar runs use the clamped absorbing
+    shell with TINY in the cleaning, and the true-y shell when
+    spec["shell"] == "true_y"."""
     import ffe
     size = tuple(spec["size"])
     path = ffe.PATH_AUTO if path is None else path
     kind = spec["kind"]
     if kind == "packet":
-        d = ffe.make_desc(size, precision=precision, path=path)
-        s = ffe.Solver(d, lib_path)
-        bg, modes, _ = alfven_packet(size, seed=spec.get("seed", 0), amp=spec.get("amp", 0.1))
-        s.init_waves(bg, modes)
-    elif kind == "tube":
-        d = ffe.make_desc(size, precision=precision, boundary=(ffe.PERIODIC, ffe.PERIODIC, ffe.OPEN),
-                          setup=ffe.SETUP_UNIFORM, params=tube_params(size, spec["beta"]), path=path)
-        s = ffe.Solver(d, lib_path)
-        s.userInitialize()
-    elif kind == "psr":
+        return ffe.make_desc(size, precision=precision, path=path)
+    if kind == "tube":
+        return ffe.make_desc(size, precision=precision, boundary=(ffe.PERIODIC, ffe.PERIODIC, ffe.OPEN),
+                             setup=ffe.SETUP_UNIFORM, params=tube_params(size, spec["beta"]), path=path)
+    if kind == "psr":
         side = size[0]
         buff = spec.get("absorb_buff", int(np.ceil(side * 48 / 512)))
         flags = ffe.FLAG_ABSORB_CLAMP | ffe.FLAG_CLEAN_TINY
         if spec.get("shell") == "true_y":
             flags |= ffe.FLAG_ABSORB_TRUE_Y
-        d = ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
-                          setup=ffe.SETUP_PSR, params=psr_params(side, spec["incl"]), path=path,
-                          flags=flags)
-        s = ffe.Solver(d, lib_path)
-        s.userInitialize()
+        return ffe.make_desc(size, precision=precision, boundary=(ffe.ABSORB,) * 3, absorb_buff=buff,
+                             setup=ffe.SETUP_PSR, params=psr_params(side, spec["incl"]), path=path, flags=flags)
+    raise ValueError("unknown run kind %r" % kind)
+
+
+def init_run(s, spec):
+    """Initial fields of a run spec on a Solver (or an oracle driven like one)
+    and the main-loop prologue."""
+    if spec["kind"] == "packet":
+        bg, modes, _ = alfven_packet(tuple(spec["size"]), seed=spec.get("seed", 0), amp=spec.get("amp", 0.1))
+        s.init_waves(bg, modes)
     else:
-        raise ValueError("unknown run kind %r" % kind)
+        s.userInitialize()
     s.mainloop_prologue()
     return s
+
+
+def build_solver(spec, precision, path=None, lib_path=None):
+    """A Solver for a run spec, initialised and past the main-loop prologue."""
+    import ffe
+    return init_run(ffe.Solver(run_desc(spec, precision, path), lib_path), spec)
