@@ -149,6 +149,7 @@ template <typename R> Absorb<R> absorb_consts(ffe_t h) {
   const R rmax = std::min(std::min(a.xc, a.yc), a.zc);
   a.rabsorb = rmax - R(h->p.absorb_buff);
   a.buff = R(h->p.absorb_buff);
+  a.inv_buff = R(1) / a.buff;
   a.clamp = (h->d.flags & FFE_FLAG_ABSORB_CLAMP) ? 1 : 0;
   a.true_y = (h->d.flags & FFE_FLAG_ABSORB_TRUE_Y) ? 1 : 0;
   return a;

@@ -54,6 +54,7 @@ template <typename R> struct CEB { const R* c[6]; };
 // Absorbing-layer constants (field_solver.F90:200-204), in precision R.
 template <typename R> struct Absorb {
   R xc, yc, zc, rabsorb, buff;
+  R inv_buff;  // 1 / buff (the fast path's quotient)
   int clamp;   // FFE_FLAG_ABSORB_CLAMP: delta_r <- min(delta_r, 1)
   int true_y;  // FFE_FLAG_ABSORB_TRUE_Y: jg = j + y0 instead of the reference's i + y0
 };

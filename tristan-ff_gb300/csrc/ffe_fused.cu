@@ -460,7 +460,10 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         else fn = e1[c * S::ENBOX + r * OW];
         w[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
-      if (ABS) absorb_cell<R>(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj0 + r, P.p.y0), p + P.p.z0, w);
+      if constexpr (ABS && FD)
+        absorb_cell_fast(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj0 + r, P.p.y0), p + P.p.z0, w);
+      else if constexpr (ABS)
+        absorb_cell<R>(P.ab, gi + P.p.x0, shell_jg(P.ab, gi, gj0 + r, P.p.y0), p + P.p.z0, w);
     };
     R v[CPT][6];
     bool frozen_cell[CPT];
@@ -826,7 +829,10 @@ __device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, i
       const R fn = STAGE1 ? f : __ldg(F.en[c] + s);
       v[c] = combine<R, C>(F.c1, F.c2, F.c3, fn, f, d[c], F.incr != 0);
     }
-    if (ABS) absorb_cell<R>(F.ab, i + F.p.x0, shell_jg(F.ab, i, j, F.p.y0), k + F.p.z0, v);
+    if constexpr (ABS && FD)
+      absorb_cell_fast(F.ab, i + F.p.x0, shell_jg(F.ab, i, j, F.p.y0), k + F.p.z0, v);
+    else if constexpr (ABS)
+      absorb_cell<R>(F.ab, i + F.p.x0, shell_jg(F.ab, i, j, F.p.y0), k + F.p.z0, v);
   }
 #pragma unroll
   for (int c = 0; c < 6; ++c) F.s1[c * n + o] = v[c];
@@ -1182,9 +1188,15 @@ template <typename R, int C>
 int fused_batch_prepare_spec_t8(int var) {
   using namespace FFE_FUSED_NS;
   constexpr int TY = FFE_BATCH_TY;
-  // only the plain variant takes the lean body (Body)
-  const int NT = var == 0 ? Body<R, C, false, false, TY>::NT : Body<R, C, true, true, TY>::NT;
-  const size_t smem = var == 0 ? Body<R, C, false, false, TY>::SMEM : Body<R, C, true, true, TY>::SMEM;
+  // per variant: the lean or the standard body (Body)
+  const int NT = var == 0   ? Body<R, C, false, false, TY>::NT
+                 : var == 1 ? Body<R, C, false, true, TY>::NT
+                 : var == 2 ? Body<R, C, true, false, TY>::NT
+                            : Body<R, C, true, true, TY>::NT;
+  const size_t smem = var == 0   ? Body<R, C, false, false, TY>::SMEM
+                      : var == 1 ? Body<R, C, false, true, TY>::SMEM
+                      : var == 2 ? Body<R, C, true, false, TY>::SMEM
+                                 : Body<R, C, true, true, TY>::SMEM;
   void (*k1)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   void (*k2)(const BatchItem*, int, const BoxTable<R>) = nullptr;
   if (var == 0) {

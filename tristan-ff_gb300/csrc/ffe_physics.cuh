@@ -161,6 +161,26 @@ __device__ __forceinline__ void absorb_cell(const Absorb<R>& ab, int ig_i, int j
   }
 }
 
+// The absorbing shell on the FP32 fast path: the same factors with the
+// hardware square-root approximation, depth (r - rabsorb) * (1 / buff), and
+// the cell test r > rabsorb - 1 made on r^2 (no root for cells inside).
+__device__ __forceinline__ float sqrt_approx(float x);
+__device__ __forceinline__ void absorb_cell_fast(const Absorb<float>& ab, int ig_i, int jg_i, int kg_i, float v[6]) {
+  const float ig = float(ig_i), jg = float(jg_i), kg = float(kg_i);
+  const float x = ig - ab.xc, y = jg - ab.yc, z = kg - ab.zc;
+  const float t = ab.rabsorb - 1.f;
+  if (t >= 0.f && !((x * x + y * y) + z * z > t * t)) return;
+  const float gx[2] = {x, x + 0.5f}, gy[2] = {y, y + 0.5f}, gz[2] = {z, z + 0.5f};
+  const int sxo[6] = {1, 0, 0, 0, 1, 1}, syo[6] = {0, 1, 0, 1, 0, 1}, szo[6] = {0, 0, 1, 1, 1, 0};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float dx = gx[sxo[c]], dy = gy[syo[c]], dz = gz[szo[c]];
+    float dr = (sqrt_approx((dx * dx + dy * dy) + dz * dz) - ab.rabsorb) * ab.inv_buff;
+    if (ab.clamp && dr > 1.f) dr = 1.f;
+    if (dr > 0.f) v[c] = (1.f - (dr * dr) * dr) * v[c];
+  }
+}
+
 // cleanEpar (field_solver.F90:288-328): E - (E.B) B / B^2 at the three E points.
 template <typename R, int C, bool FD = false>
 __device__ __forceinline__ R clean_div(R epar, R bi, R bmag, R bx, R by, R bz, R ct) {
