@@ -120,15 +120,18 @@ contains
     call ffePut(FFE_B0X, b0x); call ffePut(FFE_B0Y, b0y); call ffePut(FFE_B0Z, b0z)
   end subroutine ffeInitialize
 
+  ! c_loc needs a contiguous array: the reference's field arrays are whole
+  ! allocatable arrays, and the contiguous attribute (Fortran 2008) makes the
+  ! compiler pass them (or a contiguous copy of any other actual) as such
   subroutine ffePut(f, a)
     integer(c_int32_t), intent(in) :: f
-    real, target, intent(in) :: a(:, :, :)
+    real, target, contiguous, intent(in) :: a(:, :, :)
     call ffeCheck(ffe_upload(ffe_h, f, c_loc(a), int(size(a), c_size_t)), "ffe_upload")
   end subroutine ffePut
 
   subroutine ffeGet(f, a)
     integer(c_int32_t), intent(in) :: f
-    real, target, intent(inout) :: a(:, :, :)
+    real, target, contiguous, intent(inout) :: a(:, :, :)
     call ffeCheck(ffe_download(ffe_h, f, c_loc(a), int(size(a), c_size_t)), "ffe_download")
   end subroutine ffeGet
 
