@@ -97,3 +97,34 @@ def test_random_modes_512_fp32c_within_1e5_of_fp64(oracle_mod):
     g32.close()
     g64.close()
     assert err["E"][0] <= 1e-5 and err["B"][0] <= 1e-5, err
+
+
+def test_null_workload_fp32c_and_fp32cd_against_the_fp64_oracle(oracle_mod):
+    """Magnetic nulls (the ABC field plus waves of 1e-3, 32^3, 200 steps, TINY
+    in the cleaning): the fast FP32C and FP32CD paths against the FP64 oracle.
+    B stays within 1e-5; E (a 1e-3 perturbation, so its relative error is
+    large) within 1e-3.  The double B^2 denominators of FP32CD change the
+    error by less than a factor of two: on GB300 they cost 10x for that."""
+    from ffe.workloads import abc_nulls
+    size = (32, 32, 32)
+    bg, modes, _ = abc_nulls(size)
+    steps = 200
+    o = oracle_mod.Oracle(ffe.make_desc(size, precision=ffe.FP64, flags=ffe.FLAG_CLEAN_TINY),
+                          threads=os.cpu_count() or 1)
+    o.init_waves(bg, modes)
+    o.mainloop_prologue()
+    o.mainloop(steps, 0)
+    want = o.fields()
+    o.close()
+    err = {}
+    for prec in (ffe.FP32C, ffe.FP32CD):
+        g = ffe.Solver(ffe.make_desc(size, precision=prec, flags=ffe.FLAG_CLEAN_TINY))
+        g.init_waves(bg, modes)
+        g.mainloop_prologue()
+        g.mainloop(steps, 0)
+        err[prec] = _grouped(g.fields(), want)
+        g.close()
+    for prec, e in err.items():
+        assert e["B"][0] <= 1e-5 and e["E"][0] <= 1e-3, (prec, e)
+    ratio = err[ffe.FP32CD]["E"][0] / err[ffe.FP32C]["E"][0]
+    assert 0.5 < ratio < 2.0, err

@@ -11,6 +11,8 @@ p (a/|Kd x p|) cos(K.x + phi) and its discrete divergence vanishes.
 
   alfven_packet : Bx = 1, dBy = A sin(2 pi x / L + phi) at By's points,
                   E = -x^ x dB (v along x at c); periodic.
+  abc_nulls     : the ABC field (magnetic nulls in equilibrium) plus small
+                  seeded waves.
   random_modes  : Bz = 1 plus `n` modes with integer wavevectors
                   0 < |k| <= kmax, amplitudes U[0, amax]; the first half
                   Alfven (dB || k x z^, E = -z^ x dB), the rest fast
@@ -37,6 +39,27 @@ def alfven_packet(size=(64, 64, 64), seed=0, amp=0.1):
     phi = 2.0 * np.pi * rng.random()
     row = mode_row((1, 0, 0), size, phi, amp, p_dir=(0, 0, 1), n_dir=(1, 0, 0))
     return np.array([1.0, 0.0, 0.0]), row[None, :], {"phi": phi}
+
+
+def abc_nulls(size=(32, 32, 32), seed=3, amp=1e-3, n=6):
+    """A field with magnetic nulls in equilibrium plus small waves: the ABC
+    field with A = B = C = 1 (Bx = sin kz + cos ky, By = sin kx + cos kz,
+    Bz = sin ky + cos kx, k = 2 pi / L; a Beltrami field, curl B = k B, with
+    eight nulls per period; under the drift-only current the E that curl B
+    drives lies along B and the cleaning removes it, so the field stands)
+    and `n` seeded waves of amplitude up to `amp` (random_modes without the
+    background).  Cubic, periodic."""
+    L = size[0]
+    k = 2.0 * np.pi / L
+
+    def static(K, phi, u):  # dB = -sin(K.x + phi) u, no E
+        return np.concatenate([K, [phi, 1.0], u, [0.0, 0.0, 0.0]])
+
+    rows = [static((0, 0, k), np.pi, (1, 0, 0)), static((0, k, 0), -np.pi / 2, (1, 0, 0)),
+            static((k, 0, 0), np.pi, (0, 1, 0)), static((0, 0, k), -np.pi / 2, (0, 1, 0)),
+            static((0, k, 0), np.pi, (0, 0, 1)), static((k, 0, 0), -np.pi / 2, (0, 0, 1))]
+    _, waves, _ = random_modes(size, seed=seed, n=n, kmax=3, amax=amp)
+    return np.zeros(3), np.vstack([rows, waves]), {"amp": amp, "n": n}
 
 
 def random_modes(size=(512, 512, 512), seed=1, n=32, kmax=8, amax=0.02):
