@@ -702,7 +702,9 @@ def bench_serve(args):
         "one_grid_at_a_time_sjf": plain_sjf,
         "speedup_vs_one_at_a_time": served["cell_updates_per_s"] / plain["cell_updates_per_s"],
         "scheduler": {"epochs": srv.epochs, "batches_built": srv.batches_built, "peak_runs": srv.peak_runs,
-                      "peak_bytes": srv.peak_bytes, "budget_bytes": srv.budget},
+                      "peak_bytes": srv.peak_bytes, "budget_bytes": srv.budget,
+                      "host_s": {"wait": srv.t_wait, "admit": srv.t_admit, "build": srv.t_build,
+                                 "finish": srv.t_finish}},
         "fp64_error": errs, "gpu_launches": srv.launches,
         "config": {"workload": "%d pulsar runs, Poisson 20/s, sides U[96,256], steps U[200,2000]" % len(reqs),
                    "epoch_steps": args.epoch_steps, "max_active_cells": int(args.max_active_cells)},

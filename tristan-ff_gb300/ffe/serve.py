@@ -115,6 +115,9 @@ class Server:
         self.peak_runs = 0
         self.launches = 0
         self.log = []  # per epoch: (runs, steps, device bytes in use, cells in the batch)
+        # host seconds: waiting for epochs to finish, admitting runs (set-up on
+        # the device), rebuilding batches, and copying finished runs out
+        self.t_wait = self.t_admit = self.t_build = self.t_finish = 0.0
 
     def serve(self, requests):
         recs = sorted((Record(q) for q in requests), key=lambda r: r.arrival)
@@ -144,7 +147,9 @@ class Server:
             while queue and used + queue[0].bytes <= self.budget and (
                     not active or cells + queue[0].cells <= self.max_cells):
                 r = queue.pop(0)
+                ta = time.perf_counter()
                 r.solver = self.build(r.spec, self.precision)
+                self.t_admit += time.perf_counter() - ta
                 r.admitted = now()
                 used += r.bytes
                 cells += r.cells
@@ -154,24 +159,30 @@ class Server:
             if active:
                 ids = tuple(id(r) for r in active)
                 if ids != members:
+                    tb = time.perf_counter()
                     if batch is not None:
                         batch.close()
                     batch = self.batch_cls([r.solver for r in active])
                     batch.set_tiling(*self.tiling)
                     members = ids
                     self.batches_built += 1
+                    self.t_build += time.perf_counter() - tb
                 n = min(self.epoch_steps, min(r.steps - r.done for r in active))
                 batch.step(n, step0=[r.done for r in active])
                 self.log.append((len(active), n, used, cells))
                 self.launches += batch.launches() * n
                 self.epochs += 1
             # results of the previous epoch leave while this one computes
+            tf = time.perf_counter()
             for r in leaving:
                 _finish(r, now, self.keep)
                 used -= r.bytes
+            self.t_finish += time.perf_counter() - tf
             leaving = []
             if active:
+                tw = time.perf_counter()
                 batch.synchronize()
+                self.t_wait += time.perf_counter() - tw
                 for r in active:
                     r.done += n
                 leaving = [r for r in active if r.done >= r.steps]
