@@ -126,6 +126,33 @@ def test_fused_tiles_cover_ragged_sizes(oracle_mod):
             assert_same(g, o)
 
 
+@pytest.mark.parametrize("prec", [ffe.FP32, ffe.FP32C])
+def test_plain_fp32_tiles_cover_ragged_sizes(oracle_mod, prec):
+    """The plain FP32 variant's 32 x 12 tile (two cells per thread) on sizes
+    that are not multiples of it, below it, or leave one row of a pair:
+    the fused-exact path bit for bit, the fast path within 1e-5."""
+    sizes = [(33, 9, 5), (70, 17, 13), (2, 2, 2), (5, 31, 3), (37, 25, 14), (64, 13, 9), (31, 11, 40)]
+    for size in sizes:
+        for bnd in [(1, 1, 1), (1, 0, 1), (0, 1, 0), (0, 0, 0)]:
+            g, o = pair(oracle_mod, size, prec, bnd, ffe.PATH_FUSED_EXACT, b0=False)
+            for s in (g, o):
+                s.mainloop_prologue()
+                s.mainloop(2, 0)
+            assert_same(g, o)
+            g.close()
+            d = ffe.make_desc(size, precision=prec, boundary=bnd, path=ffe.PATH_FUSED)
+            h = ffe.Solver(d)
+            bg, modes, _ = random_modes(size, seed=5, n=6, kmax=2, amax=0.05)
+            h.init_waves(bg, modes)
+            q = oracle_mod.Oracle(d)
+            q.set_fields(h.fields())
+            for s in (h, q):
+                s.mainloop_prologue()
+                s.mainloop(3, 0)
+            assert_same(h, q, exact=False, tol=1e-5)
+            h.close()
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_waves_init_matches_host(prec):
     size = (20, 12, 10)
