@@ -11,15 +11,17 @@
 //   NEW (depth 4): updated, not yet cleaned E,B over the tile + 1 halo.
 // Per plane k:  one thread issues TMA for OLD(k+3..k+4), EN(k+2);
 //               wait OLD(k+2), EN(k+1) -> NEW(k+1) = push + update on
-//               tile+1 (the 34 x 10 region, one or two cells per thread)
-//               -> barrier -> clean plane k on the tile from
+//               tile+1 (the 34 x (TY+2) region, one or two cells per
+//               thread) -> barrier -> clean plane k on the tile from
 //               NEW(k-1..k+1), store E'' and B'.
 // With four NEW slots the clean of plane k and the push of plane k+2 touch
 // different slots, so one barrier per plane suffices and warps that have no
 // clean work move on to the next push.  A stage reads E,B (and the
 // step-start E,B for stages 2-3) once from HBM and writes E,B once; the halo
-// ring of NEW (1.33x the push work of a 32x8 tile) is recomputed instead of
-// making a second pass over memory.
+// ring of NEW (1.24x the push work of a 32 x 12 tile, 1.33x of 32 x 8) is
+// recomputed instead of making a second pass over memory.  The plain FP32
+// variant's fast path evaluates the two cells a thread owns as float2 pairs
+// with the paired FP32 instructions (see Body, ffe_physics.cuh).
 //
 // Ghosts.  The reference refreshes ghosts by exchangeFields after the update
 // and after the cleaning (src/tristanmainloop.F90:59-61).  Here a cell lying
