@@ -75,7 +75,8 @@ struct ffe_solver {
   bool maps_ok = false;   // TMA tensor maps encoded
   CUtensorMap tm_old[3][6];  // per field array: box of tile + 2 halo (stage input)
   CUtensorMap tm_en[3][6];   // per field array: box of tile + 1 halo rows (step start)
-  CUtensorMap tm_plain[3][6];  // FP32: stage-input boxes of the plain variant's taller tile
+  CUtensorMap tm_plain[3][6];     // FP32: stage-input boxes of the plain variant's taller tile
+  CUtensorMap tm_plain_en[3][6];  // FP32: its step-start boxes
   int cur = 0;
   bool has_b0 = false;
   bool ghosts_synced = false;  // all three sets hold the same ghost values
@@ -397,15 +398,16 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
       const void* mi = h->tm_old[ins[s]];
       const void* me = h->tm_en[A];
       const void* mp = h->es == 4 ? (const void*)h->tm_plain[ins[s]] : nullptr;
+      const void* mpe = h->es == 4 ? (const void*)h->tm_plain_en[A] : nullptr;
       const R ct = clean_tiny<R>(h);
       int lr;
       if (exact)
         lr = launch_fused_stage_exact<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi,
-                                            me, mp, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0,
+                                            me, mp, mpe, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0,
                                             eb_of<R>(h, outs[s]), ct, ubp, h->derr, h->st);
       else
         lr = launch_fused_stage<R, C>(h->g, h->p, ab, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1, mi, me,
-                                      mp, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
+                                      mp, mpe, ceb_of<R>(h, ins[s]), ceb_of<R>(h, A), b0, h->has_b0, eb_of<R>(h, outs[s]),
                                       ct, ubp, h->derr, h->st);
       if (lr == -4) return fail(h, FFE_EINVAL, "fused stage: the arrays of a set are not equally spaced, or no tensor maps");
       if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
@@ -674,7 +676,8 @@ int ffe_create(ffe_t* out, const ffe_grid_desc* din) {
     for (int c = 0; c < 6 && h->maps_ok; ++c)
       h->maps_ok = make_stage_maps(&h->tm_old[s][c], &h->tm_en[s][c], h->set[s][c], g, (int)h->es, FUSED_TY) == 0 &&
                    (h->es != 4 ||
-                    make_stage_maps(&h->tm_plain[s][c], nullptr, h->set[s][c], g, (int)h->es, PLAIN_TY) == 0);
+                    make_stage_maps(&h->tm_plain[s][c], &h->tm_plain_en[s][c], h->set[s][c], g, (int)h->es,
+                                    PLAIN_TY) == 0);
   if (!h->maps_ok && d.path >= FFE_PATH_FUSED) {
     cudaFreeAsync(h->arena_raw, h->st);
     cudaStreamSynchronize(h->st);

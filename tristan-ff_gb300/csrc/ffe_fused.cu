@@ -114,12 +114,14 @@ constexpr int BATCH_CPT = 1;
 // variants, the per-grid-switch batched kernel): OLD ring of 5 planes (two
 // planes of copies ahead of use), step-start fields in a 2-plane TMA ring.
 // 1, lean (the plain FP32 variant): OLD ring of 4 planes (one plane ahead),
-// step-start fields loaded by each thread for its own cells into registers
-// one plane ahead: 74 KB of shared memory at TY = 8.  NEW rows are NX words
-// in both.
+// step-start fields in a single TMA slot, refilled as soon as every thread has
+// finished the update that read it and waited for just before the next
+// update's RK combination, so that the push hides the copy: 83 KB of shared
+// memory at TY = 8, 111 KB at TY = 12 (two blocks per SM).  NEW rows are NX
+// words in both.
 template <int RK>
 struct Rings {
-  static constexpr int DO = RK == 1 ? 4 : 5, DE = RK == 0 ? 2 : 0;
+  static constexpr int DO = RK == 1 ? 4 : 5, DE = RK == 0 ? 2 : 1;
   static constexpr int NP = NX;  // NEW row pitch
 };
 
@@ -324,19 +326,19 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == PRODUCER) {  // prologue fetch: OLD kb-2 .. kb+DO-3, EN kb-1 .. kb
+  if (tid == PRODUCER) {  // prologue fetch: OLD kb-2 .. kb+DO-3, EN kb-1 .. kb+DE-2
     for (; old_next <= min(kb + DO - 3, old_last); ++old_next) issue_old(old_next);
     if (!STAGE1 && DE > 0)
-      for (; en_next <= min(kb, en_last); ++en_next) issue_en(en_next);
+      for (; en_next <= min(kb + DE - 2, en_last); ++en_next) issue_en(en_next);
   }
   // Once every thread has finished compute_new(k), the OLD slots of planes up
   // to k-1 and the EN slot of plane k are free, so OLD may run to k+DO-1 and
-  // EN to k+2.
+  // EN to k+DE.
   auto refill = [&](int k) {
     if (tid != PRODUCER) return;
     while (old_next <= old_last && old_next <= k + DO - 1) issue_old(old_next++);
     if (!STAGE1 && DE > 0)
-      while (en_next <= en_last && en_next <= k + 2) issue_en(en_next++);
+      while (en_next <= en_last && en_next <= k + DE) issue_en(en_next++);
   };
 
   // ---- consumers: rolling ring state, uniform across the block ------------
@@ -349,11 +351,17 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     if (++ow_slot == DO) { ow_slot = 0; ow_par ^= 1u; }
     return ok;
   };
-  auto wait_en = [&]() {
-    if (STAGE1 || DE == 0) return true;
-    const bool ok = mbar_wait(bar_en + 8 * (ew & 1), (unsigned)((ew >> 1) & 1), wlim);
+  // the single EN slot of the lean rings is waited for inside compute_new
+  constexpr bool EN_INNER = LEAN && !STAGE1;
+  auto wait_en_slot = [&]() {
+    if constexpr (STAGE1 || DE == 0) return true;
+    const bool ok = mbar_wait(bar_en + 8 * (ew % DE), (unsigned)((ew / DE) & 1), wlim);
     ++ew;
     return ok;
+  };
+  auto wait_en = [&]() {
+    if constexpr (EN_INNER) return true;
+    return wait_en_slot();
   };
 
   // ---- per-thread constants --------------------------------------------------
@@ -377,32 +385,15 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const int gi = x0 - 1 + nxl, gj0 = y0 - 1 + CPT * nq;
   const bool out_x = gi < 0 || gi >= g.sx;
   const R* oth = old + (CPT * nq + 1) * OW + (nxl + 1);  // cell 0 in OLD slot 0; cell r at + r * OW
-  const R* enth = en + CPT * nq * OW + (nxl + 1);        // in EN slot 0 (standard rings)
+  const R* enth = en + CPT * nq * OW + (nxl + 1);        // in EN slot 0
   R* nwth = nw + CPT * nq * NP + nxl;                    // in NEW slot 0; cell r at + r * NP
-  // Lean rings: the step-start fields of this thread's cells, read from global
-  // memory into registers one plane ahead of use: compute_new(p) consumes
-  // plane p and then issues the loads of plane p+1, which the cleaning, the
-  // barrier and the next push hide
-  constexpr bool EN_REG = LEAN && !STAGE1;
-  bool en_ok[CPT];
-  int ebase[CPT];  // in-plane offsets
-  R en_nxt[CPT][6];
-#pragma unroll
-  for (int r = 0; r < CPT; ++r) {
-    const int gj = gj0 + r;
-    en_ok[r] = cell_thread && gi >= -1 && gi <= g.sx && gj >= -1 && gj <= g.sy;
-    ebase[r] = en_ok[r] ? (gj + NG) * g.px + gi + g.ox : 0;
-  }
-  auto en_load = [&](int p) {
-    if constexpr (EN_REG) {
-#pragma unroll
-      for (int r = 0; r < CPT; ++r) {
-        const R* q = P.en0 + ((long long)(p + NG) * g.plane + ebase[r]);
-#pragma unroll
-        for (int c = 0; c < 6; ++c, q += fs) en_nxt[r][c] = en_ok[r] ? __ldg(q) : R(0);
-      }
-    }
-  };
+  // sums carried from plane to plane by the paired forms (push_pair_fast,
+  // clean_pair_fast); primed at the first plane of the chunk and after a
+  // plane that took the per-cell path
+  PushCarry pcar;
+  bool pcar_ok = false;
+  CleanCarry ccar;
+  bool ccar_ok = false;
   // B0 is read from global memory around the cell; cells of a partial tile
   // beyond the grid read around the nearest halo cell instead (their values
   // are computed but never used)
@@ -429,9 +420,12 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
                             (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
 
   // NEW(p): push + update on this thread's cells.  so = OLD slot of plane
-  // p-1, m = p - (kb - 1) (EN slot m % 2, NEW slot m % 4).
-  auto compute_new = [&](int p, int so, int m) {
-    if (!cell_thread) return;
+  // p-1, m = p - (kb - 1) (EN slot m % DE, NEW slot m % 4).  Returns false if
+  // the wait for the step-start fields (lean rings) gave up.
+  auto compute_new = [&](int p, int so, int m) -> bool {
+    if (!cell_thread) return true;
+    bool en_ready = true;
+    if constexpr (EN_INNER && !PK) en_ready = wait_en_slot();
     const int s1 = so == DO - 1 ? 0 : so + 1;
     const int s2 = s1 == DO - 1 ? 0 : s1 + 1;
     const R* o0 = oth + so * (6 * S::OLDBOX);
@@ -458,7 +452,6 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         const R f = a.b[1][c * S::OLDBOX];
         R fn;
         if constexpr (STAGE1) fn = f;
-        else if constexpr (EN_REG) fn = en_nxt[r][c];
         else fn = e1[c * S::ENBOX + r * OW];
         w[c] = combine<R, C>(c1, c2, c3, fn, f, d[c], incr);
       }
@@ -480,12 +473,18 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         a.b[1] = reinterpret_cast<const float*>(o1);
         a.b[2] = reinterpret_cast<const float*>(o2);
         float2 d[6];
-        push_pair_fast(a, (float)cc, d);
+        if (!pcar_ok) push_carry_prime(a, pcar);
+        push_pair_fast(a, (float)cc, d, pcar);
+        pcar_ok = true;
+        if constexpr (EN_INNER) en_ready = wait_en_slot();
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
           const float2 f = a(c, 0, 0, 0);
           float2 fn = f;
-          if constexpr (!STAGE1) fn = make_float2((float)en_nxt[0][c], (float)en_nxt[CPT - 1][c]);
+          if constexpr (!STAGE1) {
+            const float* q = reinterpret_cast<const float*>(e1) + c * S::ENBOX;
+            fn = make_float2(q[0], q[OW]);
+          }
           const float2 w = combine2<C>((float)c1, (float)c2, (float)c3, fn, f, d[c], incr);
           v[0][c] = (R)w.x;
           v[CPT - 1][c] = (R)w.y;
@@ -500,6 +499,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         }
       }
     } else {
+      pcar_ok = false;
+      if constexpr (EN_INNER && PK) en_ready = wait_en_slot();
 #pragma unroll
       for (int r = 0; r < CPT; ++r) {
         const int gj = gj0 + r;
@@ -567,7 +568,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     for (int r = 0; r < CPT; ++r)
 #pragma unroll
       for (int c = 0; c < 6; ++c) dst[r * NP + c * S::NEWPL] = v[r][c];
-    en_load(p + 1);
+    return en_ready;
   };
 
   // cleaned cells of this thread: (lx, CPT * lq + r) of the tile, tid < NCLEAN
@@ -603,7 +604,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       a.b[1] = reinterpret_cast<const float*>(n1);
       a.b[2] = reinterpret_cast<const float*>(n2);
       float2 e[3];
-      clean_pair_fast(a, e, 64.f * (float)ct);
+      if (!ccar_ok) clean_carry_prime(a, ccar);
+      clean_pair_fast(a, e, 64.f * (float)ct, ccar);
+      ccar_ok = true;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         v[0][c] = (R)e[c].x;
@@ -659,21 +662,22 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------
   // `failed` is block-uniform: every wait result goes through a barrier-OR.
-  en_load(kb - 1);
   bool failed = __syncthreads_or(!(wait_old() & wait_old() & wait_old() & wait_en()));  // OLD kb-2..kb, EN kb-1
   if (!failed) {
-    compute_new(kb - 1, 0, 0);
-    failed = __syncthreads_or(!(wait_old() & wait_en()));  // OLD kb+1, EN kb
+    const bool ok0 = compute_new(kb - 1, 0, 0);
+    const bool ok1 = wait_old() & wait_en();  // OLD kb+1, EN kb (standard rings)
+    failed = __syncthreads_or(!(ok0 & ok1));
     if (!failed) {
       refill(kb - 1);
-      compute_new(kb, 1, 1);
-      __syncthreads();
+      failed = __syncthreads_or(!compute_new(kb, 1, 1));
+    }
+    if (!failed) {
       // ---- march: one barrier per plane ------------------------------------
       int so = 2;  // OLD slot of plane k for compute_new(k+1)
       for (int k = kb, m = 0; k < ke; ++k, ++m) {
         refill(k);
-        const bool late = !(wait_old() & wait_en());  // OLD k+2, EN k+1
-        if (!late) compute_new(k + 1, so, m + 2);
+        bool late = !(wait_old() & wait_en());  // OLD k+2, EN k+1 (standard rings)
+        if (!late) late = !compute_new(k + 1, so, m + 2);
         if (__syncthreads_or(late)) {
           failed = true;
           break;
@@ -966,17 +970,17 @@ __global__ void k_uniform_ghosts_batch(const FixItem* __restrict__ items, const 
 
 template <typename R, int C>
 int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr, int stage,
-                    const void* maps_in, const void* maps_en, const void* maps_plain, const CEB<R>& in_g,
-                    const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
+                    const void* maps_in, const void* maps_en, const void* maps_plain, const void* maps_plain_en,
+                    const CEB<R>& in_g, const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
                     const UniformBC<R>* ub, int* err, cudaStream_t st) {
   using namespace FFE_FUSED_NS;
   const bool abs = p.bnd[0] == 2;
   // the plain FP32 variant takes the taller tile and its own stage-input maps
   const bool plain = sizeof(R) == 4 && !has_b0 && !abs;
-  if (plain && !maps_plain) return -4;
+  if (plain && (!maps_plain || !maps_plain_en)) return -4;
   Maps M;
   memcpy(M.in, plain ? maps_plain : maps_in, sizeof(M.in));
-  memcpy(M.en, maps_en, sizeof(M.en));
+  memcpy(M.en, plain ? maps_plain_en : maps_en, sizeof(M.en));
   Params<R> P;
   P.g = g;
   P.p = p;
@@ -1131,9 +1135,9 @@ int make_stage_maps(void* map_old, void* map_en, void* base, const Geom& g, int 
 
 #define FFE_INST_F(R, C)                                                                                        \
   template int FFE_LAUNCH_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, R, R, R, R, bool, int,        \
-                                     const void*, const void*, const void*, const CEB<R>&, const CEB<R>&,       \
-                                     const CEB<R>&, bool, const EB<R>&, R, const UniformBC<R>*, int*,           \
-                                     cudaStream_t);
+                                     const void*, const void*, const void*, const void*, const CEB<R>&,         \
+                                     const CEB<R>&, const CEB<R>&, bool, const EB<R>&, R, const UniformBC<R>*,  \
+                                     int*, cudaStream_t);
 #define FFE_INST_X(R, C)                                                                                        \
   template int FFE_FIX_NAME<R, C>(const Geom&, const Phys&, const Absorb<R>&, const PsrBC<R>&, R, R, R, R, bool, \
                                   int, const CEB<R>&, const CEB<R>&, const CEB<R>&, bool, const EB<R>&, R, R*,   \

@@ -56,18 +56,20 @@ void launch_finite(const Geom& g, const CEB<R>& f, int* bad, cudaStream_t st);
 // ub: the user_uniform BC constants of this step, applied inline (or null).
 // in_g / en_g: the same two sets as plain pointers (for halo cells computed at
 // their periodic image next to an open face).
-// maps_plain: the stage-input maps made for tile height PLAIN_TY, used by the
-// plain FP32 variant (no B0, no absorbing layer); null for FP64 handles.
+// maps_plain / maps_plain_en: the stage-input and step-start maps made for
+// tile height PLAIN_TY, used by the plain FP32 variant (no B0, no absorbing
+// layer); null for FP64 handles.
 template <typename R, int C>
 int launch_fused_stage(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
                        int stage, const void* maps_in, const void* maps_en, const void* maps_plain,
-                       const CEB<R>& in_g, const CEB<R>& en_g, const CEB<R>& b0, bool has_b0, const EB<R>& out, R ct,
-                       const UniformBC<R>* ub, int* err, cudaStream_t st);
+                       const void* maps_plain_en, const CEB<R>& in_g, const CEB<R>& en_g, const CEB<R>& b0,
+                       bool has_b0, const EB<R>& out, R ct, const UniformBC<R>* ub, int* err, cudaStream_t st);
 template <typename R, int C>
 int launch_fused_stage_exact(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c1, R c2, R c3, bool incr,
                              int stage, const void* maps_in, const void* maps_en, const void* maps_plain,
-                             const CEB<R>& in_g, const CEB<R>& en_g, const CEB<R>& b0, bool has_b0,
-                             const EB<R>& out, R ct, const UniformBC<R>* ub, int* err, cudaStream_t st);
+                             const void* maps_plain_en, const CEB<R>& in_g, const CEB<R>& en_g, const CEB<R>& b0,
+                             bool has_b0, const EB<R>& out, R ct, const UniformBC<R>* ub, int* err,
+                             cudaStream_t st);
 // Pulsar BC on the fused path: after a fused stage, redo the cells of the BC's
 // bounding box dilated by one (update on box+2 into s1, BC into s2, clean into
 // out).  s1, s2: 6 * (bx+4)(by+4)(bz+4) elements each.

@@ -434,41 +434,6 @@ __device__ __forceinline__ float2 xpair2(const A& a, int c, int dx, int dj, int 
 struct PointSums2 {
   float2 sa, sb, s8, s2a, s2b;
 };
-// the bare sums at the Ex, Ey, Ez points (the same neighbours as sums_x/y/z)
-template <class A>
-__device__ __forceinline__ PointSums2 sums2_x(const A& a) {
-  PointSums2 s;
-  s.s2a = f2add(a(BY, 0, 0, 0), a(BY, 0, 0, -1));
-  s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, 0, -1, 0));
-  s.sa = f2add(xpair2(a, EY, 1, 0, 0), xpair2(a, EY, 1, -1, 0));
-  s.sb = f2add(xpair2(a, EZ, 1, 0, 0), xpair2(a, EZ, 1, 0, -1));
-  s.s8 = f2add(f2add(xpair2(a, BX, 1, 0, 0), xpair2(a, BX, 1, -1, 0)),
-               f2add(xpair2(a, BX, 1, 0, -1), xpair2(a, BX, 1, -1, -1)));
-  return s;
-}
-template <class A>
-__device__ __forceinline__ PointSums2 sums2_y(const A& a) {
-  PointSums2 s;
-  s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, 0, -1));
-  s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, -1, 0, 0));
-  s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 1, 0));
-  s.sb = f2add(f2add(a(EZ, 0, 0, 0), a(EZ, 0, 1, 0)), f2add(a(EZ, 0, 0, -1), a(EZ, 0, 1, -1)));
-  s.s8 = f2add(f2add(xpair2(a, BY, -1, 0, 0), xpair2(a, BY, -1, 1, 0)),
-               f2add(xpair2(a, BY, -1, 0, -1), xpair2(a, BY, -1, 1, -1)));
-  return s;
-}
-template <class A>
-__device__ __forceinline__ PointSums2 sums2_z(const A& a) {
-  PointSums2 s;
-  s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, -1, 0));
-  s.s2b = f2add(a(BY, 0, 0, 0), a(BY, -1, 0, 0));
-  s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 0, 1));
-  s.sb = f2add(f2add(a(EY, 0, 0, 0), a(EY, 0, -1, 0)), f2add(a(EY, 0, 0, 1), a(EY, 0, -1, 1)));
-  s.s8 = f2add(f2add(xpair2(a, BZ, -1, 0, 0), xpair2(a, BZ, -1, -1, 0)),
-               f2add(xpair2(a, BZ, -1, 0, 1), xpair2(a, BZ, -1, -1, 1)));
-  return s;
-}
-
 // 64 B^2 of a point from its bare sums
 __device__ __forceinline__ float2 bmag64_2(const PointSums2& s) {
   return f2fma(s.s8, s.s8, f2mul(f2s(16.f), f2fma(s.s2a, s.s2a, f2mul(s.s2b, s.s2b))));
@@ -489,9 +454,51 @@ __device__ __forceinline__ float2 fast_current2(float cc4, float t64, float2 sr,
   return f2mul(f2mul(f2s(cc4), sr), f2rcp(f2add(bm, f2s(t64))));
 }
 
-// push_cell_fast (no B0) for two cells
+// Sums carried from plane to plane along the z march.  The eight-point B sum
+// at a point is the sum of two four-point quads in neighbouring z planes, and
+// rho at (0,0,1) is next plane's rho at (0,0,0): each is computed once, with
+// the same expression, and reused by the next plane (bit for bit the value a
+// recomputation would give).  The quads are those of Bx at the Ex point
+// (planes p, p-1), By at the Ey point (p, p-1) and Bz at the Ez point
+// (p, p+1).
+struct PushCarry {
+  float2 r0;          // rho at this plane
+  float2 qx, qy, qz;  // Bx, By quads of plane p-1; Bz quad of plane p
+};
+struct CleanCarry {
+  float2 qx, qy, qz;
+};
 template <class A>
-__device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]) {
+__device__ __forceinline__ float2 quad_x(const A& a, int dz) {  // Bx over x 0..1, y -1..0 at plane dz
+  return f2add(xpair2(a, BX, 1, 0, dz), xpair2(a, BX, 1, -1, dz));
+}
+template <class A>
+__device__ __forceinline__ float2 quad_y(const A& a, int dz) {  // By over x -1..0, y 0..1
+  return f2add(xpair2(a, BY, -1, 0, dz), xpair2(a, BY, -1, 1, dz));
+}
+template <class A>
+__device__ __forceinline__ float2 quad_z(const A& a, int dz) {  // Bz over x -1..0, y -1..0
+  return f2add(xpair2(a, BZ, -1, 0, dz), xpair2(a, BZ, -1, -1, dz));
+}
+// the carried values of a plane from its own neighbourhood (first plane of a run)
+template <class A>
+__device__ __forceinline__ void push_carry_prime(const A& a, PushCarry& c) {
+  c.r0 = rho2(a, 0, 0, 0);
+  c.qx = quad_x(a, -1);
+  c.qy = quad_y(a, -1);
+  c.qz = quad_z(a, 0);
+}
+template <class A>
+__device__ __forceinline__ void clean_carry_prime(const A& a, CleanCarry& c) {
+  c.qx = quad_x(a, -1);
+  c.qy = quad_y(a, -1);
+  c.qz = quad_z(a, 0);
+}
+
+// push_cell_fast (no B0) for two cells; `cy` holds this plane's carried values
+// on entry and the next plane's on return
+template <class A>
+__device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6], PushCarry& cy) {
   const float2 ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const float2 bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
   const float2 c2 = f2s(cc);
@@ -502,44 +509,88 @@ __device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]
   const float2 cbx = f2mul(mcc, f2sub(f2sub(by0, a(BY, 0, 0, -1)), f2sub(bz0, a(BZ, 0, -1, 0))));
   const float2 cby = f2mul(mcc, f2sub(f2sub(bz0, a(BZ, -1, 0, 0)), f2sub(bx0, a(BX, 0, 0, -1))));
   const float2 cbz = f2mul(mcc, f2sub(f2sub(bx0, a(BX, 0, -1, 0)), f2sub(by0, a(BY, -1, 0, 0))));
-  const float2 r0 = rho2(a, 0, 0, 0);
+  const float2 r0 = cy.r0;
   const float cc4 = 4.f * cc, t64 = 64.f * tiny<float>();
   float2 ea, eb, k;
   {  // X current at the Ex point (field_solver.F90:91-111): dE_x = -CC curl - k (ea s2b - s2a eb)
-    const PointSums2 s = sums2_x(a);
+    PointSums2 s;
+    s.s2a = f2add(a(BY, 0, 0, 0), a(BY, 0, 0, -1));
+    s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, 0, -1, 0));
+    s.sa = f2add(xpair2(a, EY, 1, 0, 0), xpair2(a, EY, 1, -1, 0));
+    s.sb = f2add(xpair2(a, EZ, 1, 0, 0), xpair2(a, EZ, 1, 0, -1));
+    const float2 q0 = quad_x(a, 0);
+    s.s8 = f2add(q0, cy.qx);
+    cy.qx = q0;
     k = fast_current2(cc4, t64, f2add(rho2(a, 1, 0, 0), r0), ex0, s, ea, eb);
     d[0] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbx);
   }
   {  // Y current at the Ey point (:114-134): - k (eb s2a - ea s2b)
-    const PointSums2 s = sums2_y(a);
+    PointSums2 s;
+    s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, 0, -1));
+    s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, -1, 0, 0));
+    s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 1, 0));
+    s.sb = f2add(f2add(a(EZ, 0, 0, 0), a(EZ, 0, 1, 0)), f2add(a(EZ, 0, 0, -1), a(EZ, 0, 1, -1)));
+    const float2 q0 = quad_y(a, 0);
+    s.s8 = f2add(q0, cy.qy);
+    cy.qy = q0;
     k = fast_current2(cc4, t64, f2add(rho2(a, 0, 1, 0), r0), ey0, s, ea, eb);
     d[1] = f2fma(k, f2sub(f2mul(ea, s.s2b), f2mul(eb, s.s2a)), cby);
   }
   {  // Z current at the Ez point (:137-157): - k (ea s2b - s2a eb)
-    const PointSums2 s = sums2_z(a);
-    k = fast_current2(cc4, t64, f2add(r0, rho2(a, 0, 0, 1)), ez0, s, ea, eb);
+    PointSums2 s;
+    s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, -1, 0));
+    s.s2b = f2add(a(BY, 0, 0, 0), a(BY, -1, 0, 0));
+    s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 0, 1));
+    s.sb = f2add(f2add(a(EY, 0, 0, 0), a(EY, 0, -1, 0)), f2add(a(EY, 0, 0, 1), a(EY, 0, -1, 1)));
+    const float2 q1 = quad_z(a, 1);
+    s.s8 = f2add(cy.qz, q1);
+    cy.qz = q1;
+    const float2 r1 = rho2(a, 0, 0, 1);
+    cy.r0 = r1;
+    k = fast_current2(cc4, t64, f2add(r0, r1), ez0, s, ea, eb);
     d[2] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbz);
   }
 }
 
 // clean_cell_fast for two cells (ct64 = 64 x the cleaning's TINY, 0 by default):
-// E_i - (E.B-sums) S8 / (64 B^2 + ct64)
+// E_i - (E.B-sums) S8 / (64 B^2 + ct64); `cy` as in push_pair_fast
 template <class A>
-__device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float ct64) {
+__device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float ct64, CleanCarry& cy) {
   const float2 ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const float2 c64 = f2s(ct64);
   {  // Ex point (:289-300)
-    const PointSums2 s = sums2_x(a);
+    PointSums2 s;
+    s.s2a = f2add(a(BY, 0, 0, 0), a(BY, 0, 0, -1));
+    s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, 0, -1, 0));
+    s.sa = f2add(xpair2(a, EY, 1, 0, 0), xpair2(a, EY, 1, -1, 0));
+    s.sb = f2add(xpair2(a, EZ, 1, 0, 0), xpair2(a, EZ, 1, 0, -1));
+    const float2 q0 = quad_x(a, 0);
+    s.s8 = f2add(q0, cy.qx);
+    cy.qx = q0;
     const float2 ep = f2fma(ex0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
     e[0] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ex0);
   }
   {  // Ey point (:303-314)
-    const PointSums2 s = sums2_y(a);
+    PointSums2 s;
+    s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, 0, -1));
+    s.s2b = f2add(a(BZ, 0, 0, 0), a(BZ, -1, 0, 0));
+    s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 1, 0));
+    s.sb = f2add(f2add(a(EZ, 0, 0, 0), a(EZ, 0, 1, 0)), f2add(a(EZ, 0, 0, -1), a(EZ, 0, 1, -1)));
+    const float2 q0 = quad_y(a, 0);
+    s.s8 = f2add(q0, cy.qy);
+    cy.qy = q0;
     const float2 ep = f2fma(ey0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
     e[1] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ey0);
   }
   {  // Ez point (:317-328)
-    const PointSums2 s = sums2_z(a);
+    PointSums2 s;
+    s.s2a = f2add(a(BX, 0, 0, 0), a(BX, 0, -1, 0));
+    s.s2b = f2add(a(BY, 0, 0, 0), a(BY, -1, 0, 0));
+    s.sa = f2add(xpair2(a, EX, -1, 0, 0), xpair2(a, EX, -1, 0, 1));
+    s.sb = f2add(f2add(a(EY, 0, 0, 0), a(EY, 0, -1, 0)), f2add(a(EY, 0, 0, 1), a(EY, 0, -1, 1)));
+    const float2 q1 = quad_z(a, 1);
+    s.s8 = f2add(cy.qz, q1);
+    cy.qz = q1;
     const float2 ep = f2fma(ez0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
     e[2] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ez0);
   }
