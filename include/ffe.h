@@ -77,7 +77,9 @@ typedef enum {
   FFE_FP32C = 2, /* float storage; increment-form (compensated) RK combination
                     En + (c2 (E - En) + c3 dE): no drift from 1/3 + 2/3 != 1 in float */
   FFE_FP32CD = 3 /* FFE_FP32C with the B^2 denominators of the current and of
-                    the cleaning in double (slow where FP64 is slow, as on GB300) */
+                    the cleaning in double precision: FP64 on the exact path,
+                    double-float (hi + lo float pairs, 48-bit significand) on
+                    the fast path, where FP64 arithmetic is slow (GB300)     */
 } ffe_precision;
 
 typedef enum {

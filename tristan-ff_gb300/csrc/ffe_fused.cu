@@ -139,8 +139,9 @@ template <typename R, int TY, int RK = 0> struct Sizes {
 // Configuration of the single-variant kernels (k_fused, k_fused_batch_var)
 // by element type, precision mode C, variant and tile height: the plain FP32
 // variant (no B0, no absorbing layer) takes two cells per thread and the lean
-// rings; on the fast path (C != 2) it evaluates both cells at once with the
-// paired FP32 instructions (PK), which needs up to 168 registers (two blocks
+// rings; on the fast path it evaluates both cells at once with the paired
+// FP32 instructions (PK; FP32CD with double-float denominators), which needs
+// up to 168 registers (two blocks
 // per SM); the single-grid kernel runs it at tile height PLAIN_TY (12: two
 // blocks per SM by shared memory), the batched kernels at 8, where the exact
 // path and FP32CD run at three blocks per SM (96 registers); the B0 and
@@ -152,7 +153,7 @@ template <typename R, int C, bool B0, bool ABS, int TY>
 struct Body {
   static constexpr bool LEAN = sizeof(R) == 4 && !B0 && !ABS;
   static constexpr int CPT = LEAN ? 2 : 1;
-  static constexpr bool PK = LEAN && FFE_FAST && C != 2;
+  static constexpr bool PK = LEAN && FFE_FAST;
   static constexpr int RK = LEAN ? 1 : 0;
   static constexpr int NT = Tile<TY, CPT>::NT;
   static constexpr int MINB = (PK || (LEAN && TY > 8)) ? 2 : (LEAN ? 3 : (sizeof(R) == 4 ? 2 : 1));
@@ -282,12 +283,14 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const int kb = chunk * P.kz;
   const int ke = min(kb + P.kz, g.sz);
   const bool per_x = P.p.bnd[0] == 1, per_y = P.p.bnd[1] == 1, per_z = P.p.bnd[2] == 1;
-  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  constexpr bool FD = FFE_FAST && sizeof(R) == 4;
+  constexpr bool DF = C == 2;  // FP32CD: double-float denominators
   // fast-path sums as row-grouped trees in the plain variant (whatever the
   // kernel), in the reference's order in the B0 and absorbing-layer variants
   constexpr bool TREE = !B0 && !ABS;
   // the plain FP32 variant's fast path: the two cells of a thread as float2
   // pairs through the paired FP32 instructions
+  // (FP32CD too, with DF)
   constexpr bool PK = FD && LEAN && CPT == 2;
   const R cc = P.cc, c1 = P.c1, c2 = P.c2, c3 = P.c3, ct = P.ct;
   const bool incr = P.incr != 0;
@@ -445,7 +448,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       a.dj = g.px;
       a.dk = g.plane;
       R d[6];
-      if constexpr (FD) push_cell_fast<B0, TREE>(a, cc, d);
+      if constexpr (FD) push_cell_fast<B0, TREE, SmemOld<R, TY>, DF>(a, cc, d);
       else push_cell<R, C, B0, SmemOld<R, TY>, false>(a, cc, d);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
@@ -474,7 +477,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         a.b[2] = reinterpret_cast<const float*>(o2);
         float2 d[6];
         if (!pcar_ok) push_carry_prime(a, pcar);
-        push_pair_fast(a, (float)cc, d, pcar);
+        push_pair_fast<DF>(a, (float)cc, d, pcar);
         pcar_ok = true;
         if constexpr (EN_INNER) en_ready = wait_en_slot();
 #pragma unroll
@@ -535,7 +538,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
             a.dj = g.px;
             a.dk = g.plane;
             R d[6];
-            if constexpr (FD) push_cell_fast<B0, TREE>(a, cc, d);
+            if constexpr (FD) push_cell_fast<B0, TREE, GlobalAcc<R>, DF>(a, cc, d);
             else push_cell<R, C, B0, GlobalAcc<R>, false>(a, cc, d);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
@@ -605,7 +608,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
       a.b[2] = reinterpret_cast<const float*>(n2);
       float2 e[3];
       if (!ccar_ok) clean_carry_prime(a, ccar);
-      clean_pair_fast(a, e, 64.f * (float)ct, ccar);
+      clean_pair_fast<DF>(a, e, 64.f * (float)ct, ccar);
       ccar_ok = true;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -623,7 +626,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         a.b[1] = n1 + r * NP;
         a.b[2] = n2 + r * NP;
         R e[3];
-        if constexpr (FD) clean_cell_fast<TREE>(a, e, ct);
+        if constexpr (FD) clean_cell_fast<TREE, SmemNew<R, TY, RK>, DF>(a, e, ct);
         else clean_cell<R, C, SmemNew<R, TY, RK>, false>(a, e, ct);
         v[r][0] = e[0];
         v[r][1] = e[1];
@@ -807,7 +810,8 @@ __device__ __forceinline__ bool fix_near(const FixParams<R>& F, int i, int j, in
 
 template <typename R, int C, bool B0, bool ABS, bool STAGE1>
 __device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, int bj, int bk) {
-  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  constexpr bool FD = FFE_FAST && sizeof(R) == 4;
+  constexpr bool DF = C == 2;  // FP32CD: double-float denominators
   if (bi >= F.ux || bj >= F.uy || bk >= F.uz) return;
   const int i = F.ui + bi, j = F.uj + bj, k = F.uk + bk;
   if (!fix_near(F, i, j, k, FixMargin::update)) return;
@@ -827,7 +831,7 @@ __device__ __forceinline__ void fix_update_cell(const FixParams<R>& F, int bi, i
     a.dj = g.px;
     a.dk = g.plane;
     R d[6];
-    if constexpr (FD) push_cell_fast<B0, false>(a, F.cc, d);  // the reference's order of the sums
+    if constexpr (FD) push_cell_fast<B0, false, GlobalAcc<R>, DF>(a, F.cc, d);  // the reference's order of the sums
     else push_cell<R, C, B0, GlobalAcc<R>, false>(a, F.cc, d);
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -873,7 +877,8 @@ __device__ __forceinline__ void fix_bc_cell(const FixParams<R>& F, int bi, int b
 // (bi, bj, bk): U coordinates less one (the cells of B+1 start at U + 1).
 template <typename R, int C>
 __device__ __forceinline__ void fix_clean_cell(const FixParams<R>& F, int bi, int bj, int bk) {
-  constexpr bool FD = FFE_FAST && C != 2 && sizeof(R) == 4;
+  constexpr bool FD = FFE_FAST && sizeof(R) == 4;
+  constexpr bool DF = C == 2;  // FP32CD: double-float denominators
   ++bi;
   ++bj;
   ++bk;
@@ -891,7 +896,7 @@ __device__ __forceinline__ void fix_clean_cell(const FixParams<R>& F, int bi, in
   a.dj = F.ux;
   a.dk = (long long)F.ux * F.uy;
   R e[3];
-  if constexpr (FD) clean_cell_fast<false>(a, e, F.ct);
+  if constexpr (FD) clean_cell_fast<false, BoxAcc<R>, DF>(a, e, F.ct);
   else clean_cell<R, C, BoxAcc<R>, false>(a, e, F.ct);
   const long long s = g.idx(i, j, k);
   F.out[0][s] = e[0];

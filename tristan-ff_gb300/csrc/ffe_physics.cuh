@@ -323,18 +323,61 @@ __device__ __forceinline__ PointSums sums_z(const A& a) {  // Ez point: Ex, Ey; 
           s2a, s2b};
 }
 
+// FP32CD on the fast path, one cell: the B^2 denominators as double-float
+// values (hi + lo, 48 significant bits; Dekker 1971): exact products by the
+// FMA, Knuth's TwoSum, one Newton step on the quotient.  Written with the
+// round-to-nearest intrinsics so that no add or multiply is contracted into
+// an FMA, which would break the error terms.
+struct DF1 {
+  float hi, lo;
+};
+__device__ __forceinline__ void two_sum1(float a, float b, float& s, float& t) {  // s + t == a + b
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// 64 B^2 + t from the bare sums (every term >= 0); `bm` receives 64 B^2 as a float
+__device__ __forceinline__ DF1 bmag64_df1(const PointSums& s, float t, float& bm) {
+  const float u = __fmul_rn(4.f, s.s2a), w = __fmul_rn(4.f, s.s2b);  // 16 s^2 == (4 s)^2 exactly
+  const float p1 = __fmul_rn(s.s8, s.s8), p2 = __fmul_rn(u, u), p3 = __fmul_rn(w, w);
+  const float e1 = __fmaf_rn(s.s8, s.s8, -p1), e2 = __fmaf_rn(u, u, -p2), e3 = __fmaf_rn(w, w, -p3);
+  float a, ta, tb, c, tc;
+  two_sum1(p1, p2, a, ta);
+  two_sum1(a, p3, bm, tb);
+  two_sum1(bm, t, c, tc);
+  const float lo = __fadd_rn(__fadd_rn(__fadd_rn(ta, tb), tc), __fadd_rn(__fadd_rn(e1, e2), e3));
+  DF1 r;
+  r.hi = __fadd_rn(c, lo);
+  r.lo = __fsub_rn(lo, __fsub_rn(r.hi, c));
+  return r;
+}
+// n / (d.hi + d.lo)
+__device__ __forceinline__ float df_div1(float n, const DF1& d) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d.hi));
+  const float q = __fmul_rn(n, r);
+  const float res = __fmaf_rn(-q, d.lo, __fmaf_rn(-q, d.hi, n));
+  return __fmaf_rn(res, r, q);
+}
+
+template <bool DF = false>
 __device__ __forceinline__ float fast_current(float cc4, float t64, float sr, float e0, const PointSums& s,
                                               float& ea, float& eb) {
-  const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+  float bm;
+  DF1 den;
+  if constexpr (DF) den = bmag64_df1(s, t64, bm);
+  else bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
   const float em = 64.f * (e0 * e0) + 4.f * (s.sa * s.sa + s.sb * s.sb);
   // limiter as a select: corr = 1 leaves the values unchanged exactly
   const float corr = em > bm ? sqrt_approx(__fdividef(bm, em)) : 1.f;
   ea = s.sa * corr;
   eb = s.sb * corr;
+  if constexpr (DF) return df_div1(cc4, den) * sr;
   return __fdividef(cc4, bm + t64) * sr;
 }
 
-template <bool B0, bool TREE, class A>
+// DF: the denominators of FP32CD
+template <bool B0, bool TREE, class A, bool DF = false>
 __device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6]) {
   const float ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const float bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -354,42 +397,50 @@ __device__ __forceinline__ void push_cell_fast(const A& a, float cc, float d[6])
   float ea, eb, k;
   {  // X current at the Ex point (field_solver.F90:91-111)
     const PointSums s = sums_x<TREE>(a);
-    k = fast_current(cc4, t64, a.rho(1, 0, 0) + r0, ex0, s, ea, eb);
+    k = fast_current<DF>(cc4, t64, a.rho(1, 0, 0) + r0, ex0, s, ea, eb);
     d[0] = -(cc * cbx) - k * (ea * s.s2b - s.s2a * eb);
   }
   {  // Y current at the Ey point (:114-134)
     const PointSums s = sums_y<TREE>(a);
-    k = fast_current(cc4, t64, a.rho(0, 1, 0) + r0, ey0, s, ea, eb);
+    k = fast_current<DF>(cc4, t64, a.rho(0, 1, 0) + r0, ey0, s, ea, eb);
     d[1] = -(cc * cby) - k * (eb * s.s2a - ea * s.s2b);
   }
   {  // Z current at the Ez point (:137-157)
     const PointSums s = sums_z<TREE>(a);
-    k = fast_current(cc4, t64, r0 + a.rho(0, 0, 1), ez0, s, ea, eb);
+    k = fast_current<DF>(cc4, t64, r0 + a.rho(0, 0, 1), ez0, s, ea, eb);
     d[2] = -(cc * cbz) - k * (ea * s.s2b - s.s2a * eb);
   }
 }
 
-template <bool TREE, class A>
+// E_i - ep S8 / (64 B^2 + c64) at one E point of one cell
+template <bool DF>
+__device__ __forceinline__ float clean_quot1(float ep, const PointSums& s, float c64, float e0) {
+  if constexpr (DF) {
+    float bm;
+    return e0 - df_div1(ep * s.s8, bmag64_df1(s, c64, bm));
+  }
+  const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
+  return e0 - __fdividef(ep * s.s8, bm + c64);
+}
+
+template <bool TREE, class A, bool DF = false>
 __device__ __forceinline__ void clean_cell_fast(const A& a, float e[3], float ct) {
   const float ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const float c64 = 64.f * ct;
   {  // Ex point (:289-300)
     const PointSums s = sums_x<TREE>(a);
-    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = ex0 * s.s8 + s.sa * s.s2a + s.sb * s.s2b;
-    e[0] = ex0 - __fdividef(ep * s.s8, bm + c64);
+    e[0] = clean_quot1<DF>(ep, s, c64, ex0);
   }
   {  // Ey point (:303-314)
     const PointSums s = sums_y<TREE>(a);
-    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = s.sa * s.s2a + ey0 * s.s8 + s.sb * s.s2b;
-    e[1] = ey0 - __fdividef(ep * s.s8, bm + c64);
+    e[1] = clean_quot1<DF>(ep, s, c64, ey0);
   }
   {  // Ez point (:317-328)
     const PointSums s = sums_z<TREE>(a);
-    const float bm = s.s8 * s.s8 + 16.f * (s.s2a * s.s2a + s.s2b * s.s2b);
     const float ep = s.sa * s.s2a + s.sb * s.s2b + ez0 * s.s8;
-    e[2] = ez0 - __fdividef(ep * s.s8, bm + c64);
+    e[2] = clean_quot1<DF>(ep, s, c64, ez0);
   }
 }
 
@@ -439,18 +490,63 @@ __device__ __forceinline__ float2 bmag64_2(const PointSums2& s) {
   return f2fma(s.s8, s.s8, f2mul(f2s(16.f), f2fma(s.s2a, s.s2a, f2mul(s.s2b, s.s2b))));
 }
 
+// FP32CD on the fast path: the B^2 denominators as double-float values, the
+// unevaluated sum hi + lo of two floats (48 significant bits; Dekker 1971):
+// exact products by the FMA (p = a b, e = fma(a, b, -p)), sums by Knuth's
+// TwoSum, and the quotient by one Newton step on the reciprocal estimate of
+// hi.  All of it is FP32 arithmetic in the paired instructions, where FP64
+// arithmetic runs at a small fraction of the FP32 rate.
+struct DF2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+// s + t == a + b exactly (TwoSum)
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& t) {
+  s = f2add(a, b);
+  const float2 bb = f2sub(s, a);
+  t = f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+}
+// 64 B^2 + t of a point from its bare sums as a double-float (every term is
+// >= 0); `bm` receives 64 B^2 as a float (for the limiter)
+__device__ __forceinline__ DF2 bmag64_df(const PointSums2& s, float2 t, float2& bm) {
+  const float2 u = f2mul(f2s(4.f), s.s2a), w = f2mul(f2s(4.f), s.s2b);  // 16 s^2 == (4 s)^2 exactly
+  const float2 p1 = f2mul(s.s8, s.s8), p2 = f2mul(u, u), p3 = f2mul(w, w);
+  const float2 e1 = f2fma(s.s8, s.s8, f2neg(p1)), e2 = f2fma(u, u, f2neg(p2)), e3 = f2fma(w, w, f2neg(p3));
+  float2 a, ta, tb, c, tc;
+  two_sum2(p1, p2, a, ta);
+  two_sum2(a, p3, bm, tb);
+  two_sum2(bm, t, c, tc);
+  const float2 lo = f2add(f2add(f2add(ta, tb), tc), f2add(f2add(e1, e2), e3));
+  DF2 r;
+  r.hi = f2add(c, lo);
+  r.lo = f2sub(lo, f2sub(r.hi, c));
+  return r;
+}
+// n / (d.hi + d.lo)
+__device__ __forceinline__ float2 df_div(float2 n, const DF2& d) {
+  const float2 r = f2rcp(d.hi);
+  const float2 q = f2mul(n, r);
+  const float2 res = f2fma(f2neg(q), d.lo, f2fma(f2neg(q), d.hi, n));
+  return f2fma(res, r, q);
+}
+
 // The current factor k = 4 CC Srho / (64 B^2 + 64 TINY) of a point and its
 // limited transverse E sums (ea, eb).  The limiter factor is min(1,
 // sqrt(B^2 / E^2)): 1 where E^2 <= B^2 (and where E = 0), the reference's
 // sqrt(B^2/E^2) where E^2 > B^2.
+template <bool DF>
 __device__ __forceinline__ float2 fast_current2(float cc4, float t64, float2 sr, float2 e0, const PointSums2& s,
                                                 float2& ea, float2& eb) {
-  const float2 bm = bmag64_2(s);
+  float2 bm;
+  DF2 den;
+  if constexpr (DF) den = bmag64_df(s, f2s(t64), bm);
+  else bm = bmag64_2(s);
   const float2 em = f2fma(f2mul(f2s(64.f), e0), e0, f2mul(f2s(4.f), f2fma(s.sa, s.sa, f2mul(s.sb, s.sb))));
   const float2 q = f2mul(bm, f2rcp(em));
   const float2 corr = make_float2(fminf(1.f, sqrt_approx(q.x)), fminf(1.f, sqrt_approx(q.y)));
   ea = f2mul(s.sa, corr);
   eb = f2mul(s.sb, corr);
+  if constexpr (DF) return df_div(f2mul(f2s(cc4), sr), den);
   return f2mul(f2mul(f2s(cc4), sr), f2rcp(f2add(bm, f2s(t64))));
 }
 
@@ -496,8 +592,8 @@ __device__ __forceinline__ void clean_carry_prime(const A& a, CleanCarry& c) {
 }
 
 // push_cell_fast (no B0) for two cells; `cy` holds this plane's carried values
-// on entry and the next plane's on return
-template <class A>
+// on entry and the next plane's on return; DF: the denominators of FP32CD
+template <bool DF, class A>
 __device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6], PushCarry& cy) {
   const float2 ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0), ex0 = a(EX, 0, 0, 0);
   const float2 bx0 = a(BX, 0, 0, 0), by0 = a(BY, 0, 0, 0), bz0 = a(BZ, 0, 0, 0);
@@ -521,7 +617,7 @@ __device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]
     const float2 q0 = quad_x(a, 0);
     s.s8 = f2add(q0, cy.qx);
     cy.qx = q0;
-    k = fast_current2(cc4, t64, f2add(rho2(a, 1, 0, 0), r0), ex0, s, ea, eb);
+    k = fast_current2<DF>(cc4, t64, f2add(rho2(a, 1, 0, 0), r0), ex0, s, ea, eb);
     d[0] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbx);
   }
   {  // Y current at the Ey point (:114-134): - k (eb s2a - ea s2b)
@@ -533,7 +629,7 @@ __device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]
     const float2 q0 = quad_y(a, 0);
     s.s8 = f2add(q0, cy.qy);
     cy.qy = q0;
-    k = fast_current2(cc4, t64, f2add(rho2(a, 0, 1, 0), r0), ey0, s, ea, eb);
+    k = fast_current2<DF>(cc4, t64, f2add(rho2(a, 0, 1, 0), r0), ey0, s, ea, eb);
     d[1] = f2fma(k, f2sub(f2mul(ea, s.s2b), f2mul(eb, s.s2a)), cby);
   }
   {  // Z current at the Ez point (:137-157): - k (ea s2b - s2a eb)
@@ -547,14 +643,24 @@ __device__ __forceinline__ void push_pair_fast(const A& a, float cc, float2 d[6]
     cy.qz = q1;
     const float2 r1 = rho2(a, 0, 0, 1);
     cy.r0 = r1;
-    k = fast_current2(cc4, t64, f2add(r0, r1), ez0, s, ea, eb);
+    k = fast_current2<DF>(cc4, t64, f2add(r0, r1), ez0, s, ea, eb);
     d[2] = f2fma(k, f2sub(f2mul(s.s2a, eb), f2mul(ea, s.s2b)), cbz);
   }
 }
 
+// E_i - ep S8 / (64 B^2 + c64) at one E point of two cells
+template <bool DF>
+__device__ __forceinline__ float2 clean_quot(float2 ep, const PointSums2& s, float2 c64, float2 e0) {
+  if constexpr (DF) {
+    float2 bm;
+    return f2sub(e0, df_div(f2mul(ep, s.s8), bmag64_df(s, c64, bm)));
+  }
+  return f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), e0);
+}
+
 // clean_cell_fast for two cells (ct64 = 64 x the cleaning's TINY, 0 by default):
-// E_i - (E.B-sums) S8 / (64 B^2 + ct64); `cy` as in push_pair_fast
-template <class A>
+// E_i - (E.B-sums) S8 / (64 B^2 + ct64); `cy` and DF as in push_pair_fast
+template <bool DF, class A>
 __device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float ct64, CleanCarry& cy) {
   const float2 ex0 = a(EX, 0, 0, 0), ey0 = a(EY, 0, 0, 0), ez0 = a(EZ, 0, 0, 0);
   const float2 c64 = f2s(ct64);
@@ -568,7 +674,7 @@ __device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float c
     s.s8 = f2add(q0, cy.qx);
     cy.qx = q0;
     const float2 ep = f2fma(ex0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
-    e[0] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ex0);
+    e[0] = clean_quot<DF>(ep, s, c64, ex0);
   }
   {  // Ey point (:303-314)
     PointSums2 s;
@@ -580,7 +686,7 @@ __device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float c
     s.s8 = f2add(q0, cy.qy);
     cy.qy = q0;
     const float2 ep = f2fma(ey0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
-    e[1] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ey0);
+    e[1] = clean_quot<DF>(ep, s, c64, ey0);
   }
   {  // Ez point (:317-328)
     PointSums2 s;
@@ -592,7 +698,7 @@ __device__ __forceinline__ void clean_pair_fast(const A& a, float2 e[3], float c
     s.s8 = f2add(cy.qz, q1);
     cy.qz = q1;
     const float2 ep = f2fma(ez0, s.s8, f2fma(s.sa, s.s2a, f2mul(s.sb, s.s2b)));
-    e[2] = f2fma(f2mul(ep, s.s8), f2nrcp(f2add(bmag64_2(s), c64)), ez0);
+    e[2] = clean_quot<DF>(ep, s, c64, ez0);
   }
 }
 
