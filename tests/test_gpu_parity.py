@@ -215,8 +215,8 @@ def test_errors_are_reported():
 
 
 def test_step_paths_and_launch_counts():
-    g = ffe.Solver(ffe.make_desc((16, 16, 16)))
-    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 3
+    g = ffe.Solver(ffe.make_desc((16, 16, 16)))  # stage kernel + ghost fill, three stages
+    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 6
     g = ffe.Solver(ffe.make_desc((16, 16, 16), boundary=(2, 2, 2)))
     assert g.step_path() == ffe.PATH_FUSED
     g = ffe.Solver(ffe.make_desc((16, 16, 16), boundary=(1, 1, 0)))
@@ -226,7 +226,7 @@ def test_step_paths_and_launch_counts():
     assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 12
     g = ffe.Solver(ffe.make_desc((16, 16, 16), setup=ffe.SETUP_UNIFORM, params=(8.0, 0.4, 5.0, 0.3),
                                  boundary=(1, 1, 0)))
-    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 3 + 3 * 2
+    assert g.step_path() == ffe.PATH_FUSED and g.step_launches() == 3 * (1 + 1 + 2)
     g = ffe.Solver(ffe.make_desc((16, 16, 16), setup=ffe.SETUP_LOOP, params=(4.0, 1.0, 1.0, 0.5, 5.0, 0.3),
                                  boundary=(1, 1, 0)))
     assert g.step_path() == ffe.PATH_STAGED

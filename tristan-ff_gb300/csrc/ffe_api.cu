@@ -252,10 +252,11 @@ int op_clean(ffe_t h) {
   return check_launch(h, "cleanEpar");
 }
 
+// x_done: the fused stage kernel has stored the x ghost columns
 template <typename R>
-int op_fill(ffe_t h, int s, bool with_b0) {
+int op_fill(ffe_t h, int s, bool with_b0, bool x_done = false) {
   R* b0[3] = {(R*)h->b0[0], (R*)h->b0[1], (R*)h->b0[2]};
-  launch_fill<R>(h->g, h->p, eb_of<R>(h, s), b0, with_b0, h->st);
+  launch_fill<R>(h->g, h->p, eb_of<R>(h, s), b0, with_b0, h->st, x_done);
   return check_launch(h, "exchangeFields");
 }
 
@@ -412,6 +413,9 @@ int step_fused(ffe_t h, int nsteps, int step0, bool exact) {
       if (lr == -4) return fail(h, FFE_EINVAL, "fused stage: the arrays of a set are not equally spaced, or no tensor maps");
       if (lr) return fail(h, FFE_ECUDA, "fused stage: cannot raise the shared-memory limit");
       if ((rc = check_launch(h, "fused stage"))) return rc;
+      // the periodic images of the output set (the single-grid stage kernel
+      // writes interior cells only); no launch when no axis is periodic
+      if ((rc = op_fill<R>(h, outs[s], false, true))) return rc;
       if (psr) {
         if (exact)
           launch_psr_fixup_exact<R, C>(h->g, h->p, ab, q, R(h->d.cc), R(c[0]), R(c[1]), R(c[2]), incr, s + 1,
@@ -921,13 +925,17 @@ int ffe_step_launches(ffe_t h, int32_t* n) {
   int32_t path;
   int rc;
   if ((rc = ffe_step_path(h, &path))) return rc;
+  const bool periodic = h->p.bnd[0] == 1 || h->p.bnd[1] == 1 || h->p.bnd[2] == 1;
   if (path != FFE_PATH_STAGED) {
-    // per stage: the fused kernel, plus the three box fix-up kernels of the pulsar BC
-    *n = h->d.setup == FFE_SETUP_PSR ? 12 : h->d.setup == FFE_SETUP_UNIFORM ? 3 + 3 * uniform_bc_launches(h) : 3;
+    // per stage: the fused kernel, the ghost fill of a grid with a periodic
+    // axis, the three box fix-up kernels of the pulsar BC, the ghost planes
+    // of the twisted-footpoint BC
+    const int per_stage = 1 + (periodic ? 1 : 0) + (h->d.setup == FFE_SETUP_PSR ? 3 : 0) +
+                          (h->d.setup == FFE_SETUP_UNIFORM ? uniform_bc_launches(h) : 0);
+    *n = 3 * per_stage;
     return FFE_OK;
   }
   // per stage: rho, push, update, [bc], [fill], clean + copy, [fill]
-  const bool periodic = h->p.bnd[0] == 1 || h->p.bnd[1] == 1 || h->p.bnd[2] == 1;
   int bc = 0;
   if (h->d.setup == FFE_SETUP_PSR) bc = 2;
   else if (h->d.setup == FFE_SETUP_UNIFORM) bc = 2;

@@ -76,6 +76,41 @@ constexpr int OW = TX + 4;               // OLD/EN box width (cells x0-2 .. x0+T
 constexpr int NX = TX + 2;               // NEW tile width (tile + 1 halo)
 constexpr int DN = 4;                    // NEW ring depth
 constexpr long long WAIT_LIMIT = 1LL << 22;
+// Periodic images of the cleaned cells: written by the batched kernels as they
+// clean (one launch covers many grids).  The single-grid kernels store
+// without a branch, through predicated stores: every cleaning thread stores
+// its cells (predicate: the cell lies in the grid) and, as a second set, their
+// x image (predicate: the cell lies within NG of a periodic x face; the ghost
+// columns share their 32-byte sectors with the cells stored next to them).
+// The ghost rows and planes of periodic y and z (and a second x image, when
+// sx < 2 NG) are copied by the ghost fill that follows each stage launch
+// (k_fill, whole rows).
+#if defined(FFE_BATCH_TY)
+constexpr bool KERNEL_IMAGES = true;
+#else
+constexpr bool KERNEL_IMAGES = false;
+#endif
+
+// The six components of a cell at q, q + st, ..., q + 5 st, stored only when
+// p holds (one predicate, six predicated st.global; no branch).  No memory
+// clobber: nothing in the stage kernel reads the arrays it stores to, so the
+// stores may be scheduled among the next plane's shared-memory loads.
+__device__ __forceinline__ void store6_if(bool p, float* q, long long st, const float (&v)[6]) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %0, 0;\n\t"
+      "@p st.global.f32 [%1], %7;\n\t@p st.global.f32 [%2], %8;\n\t@p st.global.f32 [%3], %9;\n\t"
+      "@p st.global.f32 [%4], %10;\n\t@p st.global.f32 [%5], %11;\n\t@p st.global.f32 [%6], %12;\n\t}"
+      ::"r"((int)p), "l"(q), "l"(q + st), "l"(q + 2 * st), "l"(q + 3 * st), "l"(q + 4 * st), "l"(q + 5 * st),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]));
+}
+__device__ __forceinline__ void store6_if(bool p, double* q, long long st, const double (&v)[6]) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %0, 0;\n\t"
+      "@p st.global.f64 [%1], %7;\n\t@p st.global.f64 [%2], %8;\n\t@p st.global.f64 [%3], %9;\n\t"
+      "@p st.global.f64 [%4], %10;\n\t@p st.global.f64 [%5], %11;\n\t@p st.global.f64 [%6], %12;\n\t}"
+      ::"r"((int)p), "l"(q), "l"(q + st), "l"(q + 2 * st), "l"(q + 3 * st), "l"(q + 4 * st), "l"(q + 5 * st),
+      "d"(v[0]), "d"(v[1]), "d"(v[2]), "d"(v[3]), "d"(v[4]), "d"(v[5]));
+}
 // probes of a wait when the test flag withholds a copy (FFE_FLAG_TEST_WITHHOLD_COPY)
 constexpr long long TEST_WAIT_LIMIT = 1LL << 14;
 
@@ -583,6 +618,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   if (per_x && ci < NG) xs[nxs++] = ci + g.sx;
   if (per_x && ci >= g.sx - NG) xs[nxs++] = ci - g.sx;
   bool c_in[CPT], xy_images[CPT];
+  // the x image stored by this thread's cells (single-grid kernels)
+  const bool x_image = per_x && (ci < NG || ci >= g.sx - NG);
+  const int x_shift = ci < NG ? g.sx : -g.sx;
   int cbase[CPT];  // in-plane offsets
 #pragma unroll
   for (int r = 0; r < CPT; ++r) {
@@ -636,6 +674,15 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
         v[r][5] = a(BZ, 0, 0, 0);
       }
     }
+#if !defined(FFE_BATCH_TY)
+    const long long po = (long long)(k + NG) * g.plane;
+#pragma unroll
+    for (int r = 0; r < CPT; ++r) {
+      R* const q = out0 + (po + cbase[r]);
+      store6_if(c_in[r], q, fs, v[r]);
+      store6_if(c_in[r] && x_image, q + x_shift, fs, v[r]);
+    }
+#else
     const bool z_image = per_z && (k < NG || k >= g.sz - NG);
 #pragma unroll
     for (int r = 0; r < CPT; ++r) {
@@ -661,6 +708,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
             for (int c = 0; c < 6; ++c) out0[o + c * fs] = v[r][c];
           }
     }
+#endif
   };
 
   // ---- prologue: NEW(kb-1), NEW(kb) ----------------------------------------

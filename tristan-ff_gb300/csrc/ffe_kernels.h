@@ -19,7 +19,8 @@ void launch_update(const Geom& g, const Phys& p, const Absorb<R>& ab, R c1, R c2
 template <typename R, int C>
 void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStream_t st);
 template <typename R>
-void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st);
+void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st,
+                 bool x_done = false);
 template <typename R>
 void launch_psr_bc(const Geom& g, const Phys& p, const PsrBC<R>& q, const EB<R>& f, R* box, cudaStream_t st);
 template <typename R>

@@ -111,48 +111,79 @@ __global__ void k_copy_e(Geom g, const R* __restrict__ dex, const R* __restrict_
 }
 
 // ---- ghost fill: the single-meshblock form of exchangeFields --------------
-// The ghost shell is enumerated as: z-slabs (k < 0 or k >= sz, all i, j),
-// y-slabs (j outside, k inside, all i), x-slabs (i outside, j, k inside).
-// A ghost is written iff every axis on which it lies outside is periodic.
+// A ghost is written iff every axis on which it lies outside is periodic; it
+// takes the value of the interior cell it wraps to on those axes.  Every
+// source is an interior cell, so the order of the writes does not matter.
+// Work items, one block each: the rows of the z-slabs (planes k < 0 and
+// k >= sz, every row j of the padded plane), the rows of the y-slabs (rows
+// j < 0 and j >= sy of every interior plane), each copied as a whole row by
+// the block's threads (coalesced), then blocks of x-slab rows: one thread per
+// interior row (j, k) writes its 2 x NG ghost cells (two 16-byte pieces at
+// the row's ends).  32-bit index arithmetic, no divisions by runtime values
+// beyond one per block.
 template <typename R>
-__global__ void k_fill(Geom g, int per_x, int per_y, int per_z, int nf, EB<R> f6, CEB<R> unused, R* b0x, R* b0y,
-                       R* b0z) {
-  const long long nxg = g.sx + 2 * NG, nyg = g.sy + 2 * NG;
-  const long long nzs = 2 * NG * nxg * nyg;              // z-slab cells
-  const long long nys = 2 * NG * nxg * (long long)g.sz;  // y-slab cells
-  const long long nxs = 2 * NG * (long long)g.sy * g.sz; // x-slab cells
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int i, j, k;
-  if (t < nzs) {
-    i = (int)(t % nxg) - NG;
-    j = (int)((t / nxg) % nyg) - NG;
-    const int kk = (int)(t / (nxg * nyg));
-    k = kk < NG ? kk - NG : g.sz + (kk - NG);
-  } else if ((t -= nzs) < nys) {
-    i = (int)(t % nxg) - NG;
-    const int jj = (int)((t / nxg) % (2 * NG));
-    j = jj < NG ? jj - NG : g.sy + (jj - NG);
-    k = (int)(t / (nxg * 2 * NG));
-  } else if ((t -= nys) < nxs) {
-    const int ii = (int)(t % (2 * NG));
-    i = ii < NG ? ii - NG : g.sx + (ii - NG);
-    j = (int)((t / (2 * NG)) % g.sy);
-    k = (int)(t / (2 * NG * (long long)g.sy));
-  } else {
+__global__ void k_fill(Geom g, int per_x, int per_y, int per_z, int nf, EB<R> f6, R* b0x, R* b0y, R* b0z,
+                       int zrows, int yrows, int xslabs) {
+  R* f[9] = {f6.c[0], f6.c[1], f6.c[2], f6.c[3], f6.c[4], f6.c[5], b0x, b0y, b0z};
+  const int nxg = g.sx + 2 * NG, nyg = g.sy + 2 * NG;
+  const int b = blockIdx.x;
+  if (b < zrows + yrows) {
+    int j, k;
+    if (b < zrows) {  // z-slab row: plane kk of the 2 NG ghost planes, row j of the padded plane
+      const int kk = b / nyg;
+      j = b - kk * nyg - NG;
+      k = kk < NG ? kk - NG : g.sz + (kk - NG);
+    } else {  // y-slab row: ghost row jj of interior plane k
+      const int e = b - zrows, jj = e % (2 * NG);
+      k = e / (2 * NG);
+      j = jj < NG ? jj - NG : g.sy + (jj - NG);
+    }
+    int sj = j, sk = k;
+    if (j < 0 || j >= g.sy) { if (!per_y) return; sj = j < 0 ? j + g.sy : j - g.sy; }
+    if (k < 0 || k >= g.sz) { if (!per_z) return; sk = k < 0 ? k + g.sz : k - g.sz; }
+    const long long dst = g.idx(-NG, j, k), src = g.idx(-NG, sj, sk);
+    for (int t = threadIdx.x; t < nxg; t += blockDim.x) {
+      const int i = t - NG;
+      int si = i;
+      if (i < 0 || i >= g.sx) { if (!per_x) continue; si = i < 0 ? i + g.sx : i - g.sx; }
+      const long long d = dst + t, s = src + (si + NG);
+      R v[9];  // every load before any store: the loads stay in flight together
+#pragma unroll
+      for (int c = 0; c < 9; ++c)
+        if (c < nf) v[c] = f[c][s];
+#pragma unroll
+      for (int c = 0; c < 9; ++c)
+        if (c < nf) f[c][d] = v[c];
+    }
     return;
   }
-  int si = i, sj = j, sk = k;
-  if (i < 0 || i >= g.sx) { if (!per_x) return; si = i < 0 ? i + g.sx : i - g.sx; }
-  if (j < 0 || j >= g.sy) { if (!per_y) return; sj = j < 0 ? j + g.sy : j - g.sy; }
-  if (k < 0 || k >= g.sz) { if (!per_z) return; sk = k < 0 ? k + g.sz : k - g.sz; }
-  const long long dst = g.idx(i, j, k), src = g.idx(si, sj, sk);
+  if (!per_x || !xslabs) return;
+  // x-slab rows
+  const int r = (b - zrows - yrows) * blockDim.x + threadIdx.x;
+  if (r >= g.sy * g.sz) return;
+  const int k = r / g.sy, j = r - k * g.sy;
+  const long long row = g.idx(0, j, k);
+  R lo[9][NG], hi[9][NG];  // every load before any store
 #pragma unroll
-  for (int c = 0; c < 6; ++c) f6.c[c][dst] = f6.c[c][src];
-  if (nf == 9) {
-    b0x[dst] = b0x[src];
-    b0y[dst] = b0y[src];
-    b0z[dst] = b0z[src];
-  }
+  for (int c = 0; c < 9; ++c)
+    if (c < nf) {
+      const R* q = f[c] + row;
+#pragma unroll
+      for (int a = 0; a < NG; ++a) {
+        lo[c][a] = q[g.sx - NG + a];  // for ghost i = a - NG (<- i + sx)
+        hi[c][a] = q[a];              // for ghost i = sx + a (<- i)
+      }
+    }
+#pragma unroll
+  for (int c = 0; c < 9; ++c)
+    if (c < nf) {
+      R* q = f[c] + row;
+#pragma unroll
+      for (int a = 0; a < NG; ++a) {
+        q[a - NG] = lo[c][a];
+        q[g.sx + a] = hi[c][a];
+      }
+    }
 }
 
 // ---- user_psr boundary condition (user/user_psr.F90:72-332) ---------------
@@ -379,16 +410,20 @@ void launch_clean(const Geom& g, const EB<R>& eb, const EB<R>& d, R ct, cudaStre
   k_copy_e<R><<<gr, B2, 0, st>>>(g, d.c[0], d.c[1], d.c[2], eb.c[0], eb.c[1], eb.c[2]);
 }
 
+// x_done: the x ghost columns of the interior rows are already filled (the
+// fused stage kernels store them), unless sx < 2 NG (two images per cell)
 template <typename R>
-void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st) {
-  if (p.bnd[0] != 1 && p.bnd[1] != 1 && p.bnd[2] != 1) return;  // nothing to wrap
-  const long long nxg = g.sx + 2 * NG, nyg = g.sy + 2 * NG;
-  const long long n = 2 * NG * nxg * nyg + 2 * NG * nxg * (long long)g.sz + 2 * NG * (long long)g.sy * g.sz;
-  const int bs = 256;
-  const unsigned nb = (unsigned)((n + bs - 1) / bs);
-  CEB<R> unused{};
-  k_fill<R><<<nb, bs, 0, st>>>(g, p.bnd[0] == 1, p.bnd[1] == 1, p.bnd[2] == 1, with_b0 ? 9 : 6, f, unused, b0[0],
-                               b0[1], b0[2]);
+void launch_fill(const Geom& g, const Phys& p, const EB<R>& f, R* const b0[3], bool with_b0, cudaStream_t st,
+                 bool x_done) {
+  const bool px = p.bnd[0] == 1, py = p.bnd[1] == 1, pz = p.bnd[2] == 1;
+  const bool xs = px && !(x_done && g.sx >= 2 * NG);
+  if (!xs && !py && !pz) return;  // nothing to wrap
+  const int zrows = pz ? 2 * NG * (g.sy + 2 * NG) : 0;
+  const int yrows = py ? 2 * NG * g.sz : 0;
+  const int bs = 128;
+  const int xblocks = xs ? (g.sy * g.sz + bs - 1) / bs : 0;
+  k_fill<R><<<(unsigned)(zrows + yrows + xblocks), bs, 0, st>>>(g, px, py, pz, with_b0 ? 9 : 6, f, b0[0], b0[1],
+                                                                  b0[2], zrows, yrows, xs ? 1 : 0);
 }
 
 template <typename R>
@@ -512,7 +547,7 @@ template int launch_waves<double>(const Geom&, const Phys&, const double[3], int
 // explicit instantiations
 #define FFE_INST_R(R)                                                                                          \
   template void launch_rho<R>(const Geom&, const R*, const R*, const R*, R*, cudaStream_t);                      \
-  template void launch_fill<R>(const Geom&, const Phys&, const EB<R>&, R* const[3], bool, cudaStream_t);         \
+  template void launch_fill<R>(const Geom&, const Phys&, const EB<R>&, R* const[3], bool, cudaStream_t, bool);         \
   template void launch_psr_bc<R>(const Geom&, const Phys&, const PsrBC<R>&, const EB<R>&, R*, cudaStream_t);     \
   template void launch_uniform_bc<R>(const Geom&, const Phys&, const UniformBC<R>&, const EB<R>&, bool,          \
                                      cudaStream_t);                                                             \
