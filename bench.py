@@ -842,7 +842,9 @@ def main():
     achieved = alg_bytes_step / (ms_per_step / 1e3) / 1e9
     traffic = traffic_from_profile(args.precision, S)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "k_fused (fused stage, %d launches/step = whole step)" % launches_per_step,
+            "traffic": traffic,
+            "kernel": "k_fused (3 fused stage launches per step) with the ghost fills after them: the whole "
+                      "step, %d launches" % launches_per_step,
             "alg_bytes_per_launch": alg_bytes_step / 3, "words_per_cell_update": WORDS_PER_CELL_STEP,
             "frac_fused_words": achieved / peak * WORDS_FUSED_PATH / WORDS_PER_CELL_STEP,
             "peak_source": peak_kind + " copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
