@@ -85,10 +85,10 @@ constexpr long long WAIT_LIMIT = 1LL << 22;
 // The ghost rows and planes of periodic y and z (and a second x image, when
 // sx < 2 NG) are copied by the ghost fill that follows each stage launch
 // (k_fill, whole rows).
-#if defined(FFE_BATCH_TY)
-constexpr bool KERNEL_IMAGES = true;
+#if defined(FFE_FUSED_EXACT)
+constexpr bool FFE_FUSED_EXACT_BUILD = true;
 #else
-constexpr bool KERNEL_IMAGES = false;
+constexpr bool FFE_FUSED_EXACT_BUILD = false;
 #endif
 
 // The six components of a cell at q, q + st, ..., q + 5 st, stored only when
@@ -296,7 +296,10 @@ struct SmemNewPair {
 // mi / me: the six tensor maps of the stage-input and step-start sets.
 // RK: ring kind (0 standard, 1 lean; see Rings).
 // Returns false when a wait on a copy gave up (the error word is set).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT, int RK>
+// PER: a grid periodic on every axis with no user BC (every plane of every
+// tile takes the uniform update path; the per-cell boundary path and the
+// twisted-footpoint BC are compiled out).
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, int CPT, int RK, bool PER = false>
 __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensorMap* me, const Params<R>& P,
                                            int tile_x, int tile_y, int chunk) {
   constexpr bool LEAN = RK == 1;
@@ -454,7 +457,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   const bool near_open_xy = (!per_x && (x0 <= 1 || x0 + TX >= g.sx - 1)) ||
                             (!per_y && (y0 <= 1 || y0 + TY >= g.sy - 1));
   // no cell of the tile has a periodic image in x or y
-  const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
+  [[maybe_unused]] const bool no_xy_images = (!per_x || (x0 >= NG && x0 + TX <= g.sx - NG)) &&
                             (!per_y || (y0 >= NG && y0 + TY <= g.sy - NG));
 
   // NEW(p): push + update on this thread's cells.  so = OLD slot of plane
@@ -501,9 +504,9 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     R v[CPT][6];
     bool frozen_cell[CPT];
     // block-uniform common case: every cell of the region is computed
-    const bool all_push = simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
+    const bool all_push = PER || (simple_xy && (per_z || (p >= 0 && p < g.sz)) &&
                           !(mixed && (touch_per_xy || (per_z && (p < 0 || p >= g.sz))) &&
-                            (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1))));
+                            (near_open_xy || (!per_z && (p <= 0 || p >= g.sz - 1)))));
     if (all_push) {
       if constexpr (PK) {
         SmemOldPair<TY> a;
@@ -591,7 +594,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     // on the planes z_glob <= 0 and >= gsz.  Frozen ghosts take the formula at
     // their own position; a halo cell on a periodic face is the image of an
     // interior cell, which took the formula at the image position.
-    if (P.ubc && (p + P.p.z0 <= 0 || p + P.p.z0 >= P.p.gsz)) {
+    if (!PER && P.ubc && (p + P.p.z0 <= 0 || p + P.p.z0 >= P.p.gsz)) {
 #pragma unroll
       for (int r = 0; r < CPT; ++r) {
         int bi = gi, bj = gj0 + r;
@@ -762,11 +765,12 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
 #if !defined(FFE_BATCH_TY)
 // One grid: block (x, y, z) = (tile_x, tile_y, z-chunk), tile height TY
 // (PLAIN_TY for the plain FP32 variant, FUSED_TY otherwise).
-template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY>
+template <typename R, int C, bool B0, bool ABS, bool STAGE1, int TY, bool PER>
 __global__ void __launch_bounds__(Body<R, C, B0, ABS, TY>::NT, Body<R, C, B0, ABS, TY>::MINB)
     k_fused(const __grid_constant__ Maps maps, const Params<R> P) {
   using CF = Body<R, C, B0, ABS, TY>;
-  stage_body<R, C, B0, ABS, STAGE1, TY, CF::CPT, CF::RK>(maps.in, maps.en, P, blockIdx.x, blockIdx.y, blockIdx.z);
+  stage_body<R, C, B0, ABS, STAGE1, TY, CF::CPT, CF::RK, PER>(maps.in, maps.en, P, blockIdx.x, blockIdx.y,
+                                                               blockIdx.z);
 }
 #else
 // Many grids in one launch.  Work item w = (grid, tile_x, tile_y, z-chunk);
@@ -1062,10 +1066,13 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
   P.kz = kz;
   const dim3 grid(tiles_x, tiles_y, (g.sz + kz - 1) / kz);
   const bool s1 = stage == 1;
-#define FFE_GO(B0V, ABSV, S1V)                                                                   \
+  // the fully periodic form of the plain FP32 variant (fast path only)
+  constexpr bool PER_OK = sizeof(R) == 4 && !FFE_FUSED_EXACT_BUILD;
+  const bool per3 = PER_OK && p.bnd[0] == 1 && p.bnd[1] == 1 && p.bnd[2] == 1 && !ub;
+#define FFE_GO(B0V, ABSV, S1V, PERV)                                                             \
   do {                                                                                           \
     constexpr int TY = (!B0V && !ABSV) ? TYP : FUSED_TY;                                         \
-    auto kf = k_fused<R, C, B0V, ABSV, S1V, TY>;                                                 \
+    auto kf = k_fused<R, C, B0V, ABSV, S1V, TY, PERV>;                                           \
     const size_t smem = Body<R, C, B0V, ABSV, TY>::SMEM;                                         \
     static bool attr_set = false;                                                                \
     if (!attr_set) {                                                                             \
@@ -1079,11 +1086,12 @@ int FFE_LAUNCH_NAME(const Geom& g, const Phys& p, const Absorb<R>& ab, R cc, R c
     kf<<<grid, Body<R, C, B0V, ABSV, TY>::NT, smem, st>>>(M, P);                                 \
   } while (0)
   if (has_b0) {
-    if (abs) { if (s1) FFE_GO(true, true, true); else FFE_GO(true, true, false); }
-    else { if (s1) FFE_GO(true, false, true); else FFE_GO(true, false, false); }
+    if (abs) { if (s1) FFE_GO(true, true, true, false); else FFE_GO(true, true, false, false); }
+    else { if (s1) FFE_GO(true, false, true, false); else FFE_GO(true, false, false, false); }
   } else {
-    if (abs) { if (s1) FFE_GO(false, true, true); else FFE_GO(false, true, false); }
-    else { if (s1) FFE_GO(false, false, true); else FFE_GO(false, false, false); }
+    if (abs) { if (s1) FFE_GO(false, true, true, false); else FFE_GO(false, true, false, false); }
+    else if (per3) { if (s1) FFE_GO(false, false, true, PER_OK); else FFE_GO(false, false, false, PER_OK); }
+    else { if (s1) FFE_GO(false, false, true, false); else FFE_GO(false, false, false, false); }
   }
 #undef FFE_GO
   return 0;
