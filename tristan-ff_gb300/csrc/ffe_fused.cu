@@ -624,6 +624,8 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
   // the x image stored by this thread's cells (single-grid kernels)
   const bool x_image = per_x && (ci < NG || ci >= g.sx - NG);
   const int x_shift = ci < NG ? g.sx : -g.sx;
+  // a tile with a cell within NG of a periodic x face (block-uniform)
+  const bool x_edge = per_x && (x0 < NG || x0 + TX > g.sx - NG);
   int cbase[CPT];  // in-plane offsets
 #pragma unroll
   for (int r = 0; r < CPT; ++r) {
@@ -683,7 +685,7 @@ __device__ __forceinline__ bool stage_body(const CUtensorMap* mi, const CUtensor
     for (int r = 0; r < CPT; ++r) {
       R* const q = out0 + (po + cbase[r]);
       store6_if(c_in[r], q, fs, v[r]);
-      store6_if(c_in[r] && x_image, q + x_shift, fs, v[r]);
+      if (x_edge) store6_if(c_in[r] && x_image, q + x_shift, fs, v[r]);
     }
 #else
     const bool z_image = per_z && (k < NG || k >= g.sz - NG);
@@ -1160,7 +1162,7 @@ void fused_tile_shape(int* tx, int* ty) {
 int fused_planes_per_block(const Geom& g, int ty) {
   const int tiles_x = (g.sx + FUSED_TX - 1) / FUSED_TX, tiles_y = (g.sy + ty - 1) / ty;
   const long long want = 152LL * 16;
-  const int kz = (int)std::max(8LL, std::min<long long>(64, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
+  const int kz = (int)std::max(8LL, std::min<long long>(96, ((long long)g.sz * tiles_x * tiles_y + want - 1) / want));
   return std::min(kz, g.sz);
 }
 
