@@ -7,7 +7,7 @@ oracle's E, B after `steps` main-loop steps (prologue first).  Cases without a
 user boundary condition are first checked bit for bit against the independent
 numpy restatement; a mismatch aborts.  The reference itself cannot run in this
 image, so these vectors pin the restatement against regressions and give the
-GPU tests a checker that needs no compiler; they do not pin it to the
+GPU tests expected values that need no compiler; they do not pin it to the
 reference's own output.
 """
 import json
